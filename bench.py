@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark of the Lagrangian-Eulerian interaction hot path on GB300.
+
+Metric: spread + interpolate markers/s (one step = bin the markers, spread
+their forces onto the staggered grid, interpolate the staggered velocity
+back onto them).  Workload: 2,000,000 markers (64 helical fibres packed in a
+0.2^3 sub-box + 400k uniform) on a 256^3 periodic staggered grid, IB_4
+kernel, mixed precision (FP32 values, FP64 positions / indices / kernel
+arguments, double-FP32 spread accumulation).  The plain FP64 form on the same
+workload, the error against it, the CPU baseline, the end-to-end rate with
+host buffers and the roofline of the dominant kernel are reported on the
+same JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: replicas only (each rank runs the whole workload on its GPU,
+value = sum over ranks, "scaling": "weak").
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "spread+interp markers/s"
+UNIT = "markers/s"
+KERNEL = "IB_4"
+KERNEL_W = 4
+N_GRID = 256
+WORKLOAD = "helices64x25k+uniform400k_256cube_IB4"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=float, default=0.1, help="fraction of markers for the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.2)
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_markers():
+    from ibamr_gb300 import workloads
+
+    X = workloads.helices_and_uniform()
+    rng = np.random.default_rng(workloads.SEED + 30)
+    F = rng.standard_normal(X.size)
+    return X, F
+
+
+def cpu_baseline(X, F, u_np, fraction, steps=2):
+    """The reference's per-patch CPU path (oracle port, one thread per slab
+    patch) on a bounded sample of the markers; markers/s."""
+    from oracle import ibx_oracle as oracle
+
+    n = X.size // 3
+    m = max(1000, int(n * fraction))
+    rng = np.random.default_rng(7)
+    sel = np.sort(rng.choice(n, size=m, replace=False))
+    Xs = np.ascontiguousarray(X.reshape(n, 3)[sel].reshape(-1))
+    Fs = np.ascontiguousarray(F.reshape(n, 3)[sel].reshape(-1))
+    cores = os.cpu_count() or 1
+    plan = oracle.CpuPlan(3, [N_GRID] * 3, KERNEL, Xs, cores)
+    f = np.zeros(3 * N_GRID ** 3)
+    U = np.zeros(Xs.size)
+    plan.step(Fs, f, u_np, U)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        plan.step(Fs, f, u_np, U)
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d markers (uniform subsample), full %d^3 grid, %d slab patches, %d timed steps"
+                      % (m, n, N_GRID, cores, steps), "ms_per_step": dt * 1e3}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    X, F = make_markers()
+    rng = np.random.default_rng(11)
+    u_np = rng.standard_normal(3 * N_GRID ** 3)
+    from oracle import ibx_oracle as oracle
+
+    n = X.size // 3
+    frac = args.cpu_sample
+    m = max(1000, int(n * frac))
+    sel = np.sort(np.random.default_rng(7).choice(n, size=m, replace=False))
+    Xs = np.ascontiguousarray(X.reshape(n, 3)[sel].reshape(-1))
+    Fs = np.ascontiguousarray(F.reshape(n, 3)[sel].reshape(-1))
+    cores = os.cpu_count() or 1
+    plan = oracle.CpuPlan(3, [N_GRID] * 3, KERNEL, Xs, cores)
+    f = np.zeros(3 * N_GRID ** 3)
+    U = np.zeros(Xs.size)
+    for _ in range(args.warmup):
+        plan.step(Fs, f, u_np, U)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.step(Fs, f, u_np, U)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = m / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "markers": n, "grid": [N_GRID] * 3, "kernel": KERNEL},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d of %d markers per step (uniform subsample), %d slab patches" % (m, n, cores)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from ibamr_gb300 import ibx, workloads
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    ibx.lib()
+    X, F = make_markers()
+    n = X.size // 3
+    N = [N_GRID] * 3
+    dx = [1.0 / N_GRID] * 3
+    rng = np.random.default_rng(11)
+    u_np = rng.standard_normal(3 * N_GRID ** 3)
+    stream = torch.cuda.current_stream()
+
+    X_t = torch.tensor(X, device=dev)
+    F_t = torch.tensor(F, dtype=torch.float32, device=dev)
+    U_t = torch.zeros(3 * n, dtype=torch.float32, device=dev)
+    f_t = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
+    u_t = [torch.tensor(u_np.reshape(3, *N)[a], dtype=torch.float32, device=dev) for a in range(3)]
+
+    def prob(q, Xq, Q):
+        return ibx.make_problem(3, ibx.SIDE, ibx.MODE_PERIODIC, [0] * 3, [N_GRID - 1] * 3, dx, [0.0] * 3, [1.0] * 3,
+                                q, Xq, Q)
+
+    plan = ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)])
+
+    def step():
+        plan.bin()
+        plan.spread()
+        plan.interpolate()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3)
+    launches_per_step = 3 + 3 + 2 + 1 + 1  # bin, scan x2 (<=3 each), scatter, spread, interp
+
+    # ---- per-phase timing (same stream) for the roofline --------------------
+    def timed(fn, reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    reps = max(3, args.steps // 2)
+    t_bin = timed(plan.bin, reps)
+    t_spread = timed(plan.spread, reps)
+    t_interp = timed(plan.interpolate, reps)
+    T = workloads.touched_faces(X, 3, N, KERNEL_W)
+    s_v = s_g = 4
+    b_spread = n * 3 * (8 + s_v) + T * 2 * s_g
+    b_interp = n * 3 * (8 + s_v) + T * s_g
+    b_step = n * 3 * (8 + 2 * s_v) + T * 3 * s_g
+    peak, peak_kind = measured_peak()
+    dom = max([("spread", t_spread, b_spread), ("interpolate", t_interp, b_interp), ("bin", t_bin, 0)],
+              key=lambda z: z[1])
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom[0])
+        except Exception:
+            traffic = None
+    achieved = (dom[2] / (dom[1] * 1e-3)) / 1e9 if dom[2] else 0.0
+    roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "step_achieved": (b_step / (ms * 1e-3)) / 1e9, "step_frac": (b_step / (ms * 1e-3)) / 1e9 / peak,
+                "algorithmic_bytes": {"spread": b_spread, "interpolate": b_interp, "step": b_step,
+                                      "touched_faces": T}}
+
+    # ---- accuracy of the mixed form against the plain FP64 form -------------
+    f_t2 = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
+    plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED)
+    plan_e.bin()
+    plan_e.spread()
+    fd = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
+    ud = [t.double() for t in u_t]
+    Fd = torch.tensor(F, device=dev)
+    Ud = torch.zeros(3 * n, dtype=torch.float64, device=dev)
+    ibx.spread(prob(fd, X_t, Fd), KERNEL, ibx.FP64)
+    ibx.interpolate(prob(ud, X_t, Ud), KERNEL, ibx.FP64)
+    torch.cuda.synchronize()
+    err_f = max(float((f_t2[a].double() - fd[a]).abs().max()) for a in range(3)) / max(
+        float(fd[a].abs().max()) for a in range(3))
+    plan.interpolate()
+    torch.cuda.synchronize()
+    err_U = float((U_t.double() - Ud).abs().max() / Ud.abs().max())
+    plan_e.close()
+
+    # ---- plain FP64 form (marker-parallel, FP64 atomics) on the same workload --
+    def step_plain():
+        ibx.spread(prob(fd, X_t, Fd), KERNEL, ibx.FP64)
+        ibx.interpolate(prob(ud, X_t, Ud), KERNEL, ibx.FP64)
+
+    step_plain()
+    k_plain = max(2, args.steps // 5)
+    ms_plain = timed(step_plain, k_plain)
+    del fd, ud, Fd, Ud
+
+    # ---- end to end through the public API with host buffers ----------------
+    Xh = torch.tensor(X).pin_memory()
+    Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
+    Uh = torch.empty(3 * n, dtype=torch.float32).pin_memory()
+
+    def step_e2e():
+        X_t.copy_(Xh, non_blocking=True)
+        F_t.copy_(Fh, non_blocking=True)
+        step()
+        Uh.copy_(U_t, non_blocking=True)
+
+    for _ in range(2):
+        step_e2e()
+    barrier()
+    ms_e2e = timed(step_e2e, args.steps)
+    if world > 1:
+        t = torch.tensor([ms_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": X.size * 8 + F.size * 4,
+           "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e}
+
+    cpu = cpu_baseline(X, F, u_np, args.cpu_sample) if rank == 0 else None
+    plan.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "markers": n, "grid": N, "kernel": KERNEL, "centering": "side",
+                       "precision": "mixed", "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
+            "plain_fp64": {"value": n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+            "mixed_vs_plain": ms_plain / ms,
+            "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

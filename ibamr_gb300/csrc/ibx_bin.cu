@@ -1,0 +1,420 @@
+// ibx_bin.cu -- marker binning of the plan pipeline: exact stencil indices,
+// integer counting sort by tile, work items of the tiled spread.
+//
+// Index arithmetic.  The reference computes t = (X + Xshift - x_lower)/dx in
+// FP64 and takes NINT(t) (IB_4, IB_6), floor(t) (IB_3, PIECEWISE_CUBIC,
+// BSPLINE_4) or NINT(t - 1/2) plus a half-cell test (PIECEWISE_LINEAR)
+// (F3D:1265-1293, 2244-2330, 808-840, 305-330).  GB300 executes FP64 at
+// about 1/70 of the FP32 rate, so t is formed here in 64-bit fixed point on
+// the integer pipe: Xf = floor(X*2^sx) from the bits of X, D = Xf - xlo_f,
+// T = mulhi(D, inv_f), t = T/2^F with |t - t_real| < 2^-44.  The FP64 value
+// the reference rounds differs from t_real by a few ulps of t, so every
+// decision (integer and half-integer crossings) is taken from T unless T
+// lies within a margin of 16 ulps of the largest t of the problem from a
+// decision boundary; those rare markers (and any position outside the
+// fixed-point range) are recomputed with the reference's FP64 expressions.
+// Either way the stencil indices are bit-identical to the reference's.
+
+#include "ibx_plan.cuh"
+#include "../../include/ibx.h"
+
+namespace ibx
+{
+namespace
+{
+// floor(x * 2^S) for |x| * 2^S < 2^62; ok = false otherwise (or non-finite).
+__device__ __forceinline__ long long
+to_fixed(double x, int S, bool& ok)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    ok = false;
+    if (e == 0x7FF) return 0;
+    unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    int ee = e;
+    if (e)
+        m |= 1ull << 52;
+    else
+        ee = 1;
+    const int sh = ee - 1075 + S; // x*2^S = m * 2^sh
+    unsigned long long v;
+    bool exact;
+    if (sh >= 0)
+    {
+        if (sh > 9) return 0; // |x|*2^S >= 2^62
+        v = m << sh;
+        exact = true;
+    }
+    else
+    {
+        const int r = -sh;
+        if (r >= 64)
+        {
+            v = 0;
+            exact = m == 0;
+        }
+        else
+        {
+            v = m >> r;
+            exact = (m & ((1ull << r) - 1)) == 0;
+        }
+    }
+    long long out = (long long)v;
+    if (b >> 63) out = -out - (exact ? 0 : 1);
+    ok = true;
+    return out;
+}
+
+// Exact stencil base and r_first by the reference's FP64 expressions (the
+// fallback; see stencil_fp64 in ibx_device.cuh for the per-kernel rules).
+template <int K>
+__device__ __noinline__ void
+base_r_fp64(double X, double xlo, double dx, double inv_dx, int pow2, int& base, float& rfirst)
+{
+    const double v = __dsub_rn(X, xlo);
+    const double t = clamp_index_arg(pow2 ? __dmul_rn(v, inv_dx) : __ddiv_rn(v, dx));
+    if (K == K_IB4)
+        base = nint_exact(t) - 2;
+    else if (K == K_IB6)
+        base = nint_exact(t) - 3;
+    else if (K == K_PL)
+    {
+        const int icc = nint_exact(__dsub_rn(t, 0.5));
+        base = (X < cell_center(icc, xlo, dx)) ? icc - 1 : icc;
+    }
+    else
+    {
+        const int icc = (int)floor(t);
+        if (K == K_IB3)
+            base = icc - 1;
+        else
+            base = (X < cell_center(icc, xlo, dx)) ? icc - 2 : icc - 1;
+    }
+    rfirst = (float)(t - ((double)base + 0.5));
+}
+
+// Base and r_first from the fixed-point t; returns false when t is within
+// the margin of a decision boundary.
+template <int K>
+__device__ __forceinline__ bool
+base_r_fixed(long long Xf, long long xlo_f, long long inv_f, int F, int dshift, int& base, float& rfirst)
+{
+    const long long D = Xf - xlo_f;
+    const long long T = __mul64hi(D, inv_f);
+    const long long one = 1ll << F;
+    const long long half = one >> 1;
+    const long long fr = T & (one - 1);
+    const long long dl = 1ll << dshift;
+    if (fr < dl || fr > one - dl || (fr > half - dl && fr < half + dl)) return false;
+    const int ip = (int)(T >> F);
+    const bool up = fr >= half;
+    if (K == K_IB4)
+        base = ip + (up ? 1 : 0) - 2;
+    else if (K == K_IB6)
+        base = ip + (up ? 1 : 0) - 3;
+    else if (K == K_PL)
+        base = up ? ip : ip - 1;
+    else if (K == K_IB3)
+        base = ip - 1;
+    else
+        base = up ? ip - 1 : ip - 2;
+    const long long rf = T - ((long long)base << F) - half;
+    rfirst = __ll2float_rn(rf) * __int_as_float((127 - F) << 23);
+    return true;
+}
+
+// Warp-aggregated counter increment: lanes with equal keys share one atomic;
+// returns the old value plus the lane's rank among them.
+__device__ __forceinline__ int
+agg_add(int* counters, int key, bool valid)
+{
+    const unsigned act = __ballot_sync(__activemask(), valid);
+    int res = 0;
+    if (valid)
+    {
+        const unsigned grp = __match_any_sync(act, key);
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(grp) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&counters[key], __popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        res = base + __popc(grp & ((1u << lane) - 1));
+    }
+    return res;
+}
+
+// Distinct tiles (along one dim) holding the cells (b+i) mod N, i in [0, span).
+__device__ __forceinline__ int
+tiles_1d(int b, int span, int N, int E, int* out)
+{
+    int n = 0;
+    for (int i = 0; i < span; ++i)
+    {
+        const int tile = wrap_cell(b + i, N) / E;
+        bool seen = false;
+        for (int k = 0; k < n; ++k) seen = seen || out[k] == tile;
+        if (!seen && n < 4) out[n++] = tile;
+    }
+    return n;
+}
+
+template <int DIM, int K>
+__device__ __forceinline__ int
+visit_tiles(const PlanProb& P, const Rec& R, int (*tl)[4], int* nt)
+{
+    constexpr int W = KT<K>::W;
+    constexpr int E = TileT<DIM>::E;
+    int total = 1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        if (d >= DIM)
+        {
+            nt[d] = 1;
+            tl[d][0] = 0;
+            continue;
+        }
+        const int lo = P.side ? min((int)R.bc[d], (int)R.bs[d]) : R.bc[d];
+        const int hi = (P.side ? max((int)R.bc[d], (int)R.bs[d]) : R.bc[d]) + W - 1;
+        nt[d] = tiles_1d(lo, hi - lo + 1, P.N[d], E, tl[d]);
+        total *= nt[d];
+    }
+    return total;
+}
+
+template <int DIM>
+__device__ __forceinline__ int
+visit_tile_id(const PlanProb& P, int (*tl)[4], const int* nt, int k)
+{
+    const int c0 = k % nt[0];
+    const int c1 = (k / nt[0]) % nt[1];
+    const int c2 = DIM == 3 ? k / (nt[0] * nt[1]) : 0;
+    return P.tile0 + tl[0][c0] + P.ntile[0] * (tl[1][c1] + P.ntile[1] * tl[2][c2]);
+}
+
+template <int DIM, int K>
+__global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
+{
+    constexpr int W = KT<K>::W;
+    constexpr int E = TileT<DIM>::E;
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool valid = g < D.n_markers;
+    const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
+    const PlanProb& P = D.probs[p];
+    Rec R;
+    int home[3] = { 0, 0, 0 };
+    if (valid)
+    {
+        const long long s = g - P.marker0;
+        bool finite = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+            if (d >= DIM)
+            {
+                R.bc[d] = R.bs[d] = 0;
+                R.rc[d] = R.rs[d] = 0.f;
+                continue;
+            }
+            const double X = P.X[DIM * s + d];
+            finite = finite && isfinite(X);
+            const FixedDim& fx = P.fx[d];
+            int bc, bs;
+            float rc, rs;
+            bool ok = P.fixed_ok != 0;
+            long long Xf = 0;
+            if (ok) Xf = to_fixed(X, fx.sx, ok);
+            if (!(ok && base_r_fixed<K>(Xf, fx.xlo_c_f, fx.inv_f, fx.F, fx.dshift, bc, rc)))
+                base_r_fp64<K>(X, P.xlo_c[d], P.dx[d], P.inv_dx[d], P.dx_pow2[d], bc, rc);
+            if (!(ok && base_r_fixed<K>(Xf, fx.xlo_s_f, fx.inv_f, fx.F, fx.dshift, bs, rs)))
+                base_r_fp64<K>(X, P.xlo_s[d], P.dx[d], P.inv_dx[d], P.dx_pow2[d], bs, rs);
+            // Periodic domain: move both bases by the multiple of N that puts bc in [0, N).
+            const int N = P.N[d];
+            const int shift = (bc >= 0 ? bc / N : -((-bc + N - 1) / N)) * N;
+            bc -= shift;
+            bs -= shift;
+            R.bc[d] = (short)bc;
+            R.bs[d] = (short)bs;
+            R.rc[d] = rc;
+            R.rs[d] = rs;
+            home[d] = wrap_cell(bc + (W - 1) / 2, N) / E;
+        }
+        if (!finite)
+        {
+            // Reported through the plan's status word; the marker is skipped.
+            atomicOr(D.status, 1);
+            D.home_tile[g] = -1;
+            valid = false;
+        }
+    }
+    int ht = 0, tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    if (valid)
+    {
+        D.rec[g] = R;
+        ht = P.tile0 + home[0] + P.ntile[0] * (home[1] + (DIM == 3 ? P.ntile[1] * home[2] : 0));
+        D.home_tile[g] = ht;
+        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+    }
+    agg_add(D.hcount, ht, valid);
+    for (int k = 0; __any_sync(0xffffffff, k < nvis); ++k)
+    {
+        const bool v = k < nvis;
+        agg_add(D.vcount, v ? visit_tile_id<DIM>(P, tl, nt, k) : 0, v);
+    }
+}
+
+template <int DIM, int K>
+__global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
+{
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool valid = g < D.n_markers;
+    const int ht = valid ? D.home_tile[g] : -1;
+    valid = valid && ht >= 0;
+    const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
+    const PlanProb& P = D.probs[p];
+    int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    if (valid)
+    {
+        const Rec R = D.rec[g];
+        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+    }
+    const int hp = agg_add(D.hcursor, valid ? ht : 0, valid);
+    if (valid) D.home_list[D.hcount[ht] + hp] = (int)g;
+    for (int k = 0; __any_sync(0xffffffff, k < nvis); ++k)
+    {
+        const bool v = k < nvis;
+        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
+        const int r = agg_add(D.vcursor, t, v);
+        if (v)
+        {
+            const long long pos = (long long)D.vcount[t] + r;
+            if (pos < D.n_visit_cap)
+                D.visit_list[pos] = (int)g;
+            else
+                atomicOr(D.status, 2);
+        }
+    }
+}
+// ---- exclusive scan (two levels, exact integer) ---------------------------
+constexpr int SCAN_BLOCK = 1024;
+constexpr int SCAN_ITEMS = 2048; // elements per block
+
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_blocks(int* data, int n, int* block_sums)
+{
+    __shared__ int s[SCAN_ITEMS];
+    const int base = blockIdx.x * SCAN_ITEMS;
+    for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_BLOCK) s[i] = (base + i < n) ? data[base + i] : 0;
+    // Blelloch up-sweep / down-sweep.
+    int offset = 1;
+    for (int d = SCAN_ITEMS >> 1; d > 0; d >>= 1)
+    {
+        __syncthreads();
+        if (threadIdx.x < d)
+        {
+            const int ai = offset * (2 * threadIdx.x + 1) - 1;
+            const int bi = offset * (2 * threadIdx.x + 2) - 1;
+            s[bi] += s[ai];
+        }
+        offset <<= 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        if (block_sums) block_sums[blockIdx.x] = s[SCAN_ITEMS - 1];
+        s[SCAN_ITEMS - 1] = 0;
+    }
+    for (int d = 1; d < SCAN_ITEMS; d <<= 1)
+    {
+        offset >>= 1;
+        __syncthreads();
+        if (threadIdx.x < d)
+        {
+            const int ai = offset * (2 * threadIdx.x + 1) - 1;
+            const int bi = offset * (2 * threadIdx.x + 2) - 1;
+            const int t = s[ai];
+            s[ai] = s[bi];
+            s[bi] += t;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_BLOCK)
+        if (base + i < n) data[base + i] = s[i];
+}
+
+__global__ void scan_add(int* data, int n, const int* block_offsets)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) data[i] += block_offsets[i / SCAN_ITEMS];
+}
+
+// Spread work items: a tile with c visits gets ceil(c / item_visits) items.
+__global__ void items_count(const DevPlan D)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= D.n_tiles) return;
+    const int c = D.vcount[t + 1] - D.vcount[t];
+    D.items[t] = (c + D.item_visits - 1) / D.item_visits;
+}
+
+__global__ void items_fill(const DevPlan D)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= D.n_tiles) return;
+    for (int k = D.items[t]; k < D.items[t + 1] && k < D.n_item_cap; ++k) D.item_tile[k] = t;
+}
+} // namespace
+
+// Exclusive scan of data[0..n) in place; tmp holds SCAN_ITEMS ints.
+int
+exclusive_scan(int* data, int n, int* tmp, cudaStream_t s)
+{
+    const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
+    if (nb > SCAN_ITEMS) return IBX_E_TOO_LARGE; // more than 4M entries
+    scan_blocks<<<nb, SCAN_BLOCK, 0, s>>>(data, n, tmp);
+    if (nb > 1)
+    {
+        scan_blocks<<<1, SCAN_BLOCK, 0, s>>>(tmp, nb, nullptr);
+        scan_add<<<(n + 255) / 256, 256, 0, s>>>(data, n, tmp);
+    }
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+int
+launch_items(const DevPlan& D, cudaStream_t s)
+{
+    const int blocks = (D.n_tiles + 255) / 256;
+    items_count<<<blocks, 256, 0, s>>>(D);
+    if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
+    // items[n_tiles] was zeroed with the counters; the scan turns counts into offsets.
+    return IBX_OK;
+}
+
+int
+launch_items_fill(const DevPlan& D, cudaStream_t s)
+{
+    items_fill<<<(D.n_tiles + 255) / 256, 256, 0, s>>>(D);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+int
+launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter)
+{
+    const unsigned blocks = (unsigned)((D.n_markers + 255) / 256);
+    if (blocks == 0) return IBX_OK;
+#define IBX_BIN_CASE(DD, KK)                                                                                         \
+    if (dim == DD && kernel == KK)                                                                                   \
+    {                                                                                                                \
+        if (scatter)                                                                                                 \
+            scatter_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                        \
+        else                                                                                                         \
+            bin_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                            \
+        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
+    }
+    IBX_BIN_CASE(2, K_PL) IBX_BIN_CASE(2, K_PCUBIC) IBX_BIN_CASE(2, K_IB3) IBX_BIN_CASE(2, K_IB4)
+    IBX_BIN_CASE(2, K_IB6) IBX_BIN_CASE(2, K_BSPL4) IBX_BIN_CASE(3, K_PL) IBX_BIN_CASE(3, K_PCUBIC)
+    IBX_BIN_CASE(3, K_IB3) IBX_BIN_CASE(3, K_IB4) IBX_BIN_CASE(3, K_IB6) IBX_BIN_CASE(3, K_BSPL4)
+#undef IBX_BIN_CASE
+    return IBX_E_BAD_KERNEL;
+}
+
+} // namespace ibx

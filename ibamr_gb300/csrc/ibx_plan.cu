@@ -1,0 +1,368 @@
+// ibx_plan.cu -- host side of the binned spread / interpolate pipeline
+// (ibx_plan_* in include/ibx.h).
+//
+// Per step:
+//   1. bin (ibx_bin.cu): one thread per marker derives the exact stencil
+//      bases and kernel arguments (cell-centred and staggered position) and
+//      counts the marker into its home tile and into every tile its
+//      footprint touches (warp-aggregated atomics).
+//   2. exclusive scans of both histograms (exact integer).
+//   3. scatter: counting sort into per-tile home lists and visit lists.
+//   4. work items: tiles with many visits are split into several items.
+//   5. spread (ibx_spread.cu): one CTA per work item owns its tile.
+//   6. interpolate (ibx_interp.cu): markers in home-tile order.
+// Geometry: IBX_MODE_PERIODIC problems (compact periodic arrays).
+
+#include "ibx_plan.cuh"
+#include "../../include/ibx.h"
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace ibx
+{
+int build_prob(const ibx_problem& in, int kernel, bool spread, Prob& P);
+
+namespace
+{
+constexpr int ITEM_VISITS = 2048; // default visits per spread work item
+
+int
+item_visits_setting()
+{
+    // IBX_ITEM_VISITS overrides the default (tuning knob; >= 256).
+    const char* e = std::getenv("IBX_ITEM_VISITS");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 256 ? v : ITEM_VISITS;
+}
+
+int
+ceil_log2(long double v)
+{
+    int e = 0;
+    while (std::ldexp(1.0L, e) < v) ++e;
+    return e;
+}
+
+// Constants of the exact fixed-point index path for one dimension (see
+// ibx_bin.cu); returns false when the problem's range does not fit.
+bool
+fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx)
+{
+    const long double xmax = 2.0L * std::max(std::fabs((long double)x_lower), std::fabs((long double)x_upper)) +
+                             8.0L * dx + 1e-30L;
+    fx.sx = 62 - ceil_log2(xmax);
+    const long double inv = 1.0L / (long double)dx;
+    const int si = 62 - (std::ilogb(inv) + 1);
+    fx.inv_f = std::llround(std::ldexp(inv, si));
+    fx.F = fx.sx + si - 64;
+    const int tb = ceil_log2(xmax * inv + 2.0L);
+    fx.dshift = fx.F - 48 + tb;
+    fx.xlo_c_f = std::llround(std::ldexp((long double)x_lower, fx.sx));
+    const double xlo_s = x_lower - 0.5 * dx; // the reference's FP64 side-axis origin
+    fx.xlo_s_f = std::llround(std::ldexp((long double)xlo_s, fx.sx));
+    return fx.sx > 0 && fx.F >= 24 && fx.F <= 62 && fx.dshift >= 2 && fx.dshift <= fx.F - 4 && tb <= 30;
+}
+
+size_t
+align256(size_t v)
+{
+    return (v + 255) & ~size_t(255);
+}
+} // namespace
+} // namespace ibx
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+struct ibx_plan
+{
+    int dim, kernel, precision, n_probs, max_ncomp;
+    ibx::DevPlan D;
+    void* dmem;
+    size_t dbytes;
+    int* scan_tmp;
+};
+
+extern "C" {
+
+int
+ibx_plan_create(const ibx_problem* problems, int n_problems, int kernel, int precision, ibx_plan** out)
+{
+    return ibx_plan_create2(problems, problems, n_problems, kernel, precision, out);
+}
+
+int
+ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
+                 int precision, ibx_plan** out)
+{
+    using namespace ibx;
+    if (!out) return IBX_E_ARG;
+    *out = nullptr;
+    if (!problems || !interp_problems || n_problems < 1) return IBX_E_ARG;
+    if (kernel < IBX_KERNEL_PIECEWISE_LINEAR || kernel > IBX_KERNEL_BSPLINE_4) return IBX_E_BAD_KERNEL;
+    if (precision != IBX_PRECISION_MIXED) return IBX_E_ARG;
+    const int dim = problems[0].dim;
+    std::vector<PlanProb> hp(n_problems);
+    std::vector<long long> moffs(n_problems + 1, 0);
+    std::vector<int> toffs(n_problems + 1, 0);
+    long long visit_cap = 0;
+    int max_ncomp = 1;
+    const int E = dim == 3 ? TILE3 : TILE2;
+    for (int p = 0; p < n_problems; ++p)
+    {
+        const ibx_problem& in = problems[p];
+        Prob chk;
+        const int rc = build_prob(in, kernel, true, chk);
+        if (rc) return rc;
+        if (in.dim != dim || in.mode != IBX_MODE_PERIODIC) return IBX_E_ARG;
+        if (in.indices || in.Xshift) return IBX_E_ARG; // periodic plans take every marker
+        const int ncomp = in.centering == IBX_SIDE ? dim : in.q_depth;
+        if (ncomp > 3) return IBX_E_TOO_LARGE;
+        max_ncomp = ncomp > max_ncomp ? ncomp : max_ncomp;
+        PlanProb& P = hp[p];
+        std::memset(&P, 0, sizeof(P));
+        P.dim = dim;
+        P.ncomp = ncomp;
+        P.side = in.centering == IBX_SIDE;
+        P.Q_depth = in.Q_depth;
+        long long ntiles = 1, vol = 1, per = 1;
+        for (int d = 0; d < 3; ++d)
+        {
+            if (d >= dim)
+            {
+                P.N[d] = 1;
+                P.ntile[d] = 1;
+                P.dx[d] = P.inv_dx[d] = 1.0;
+                continue;
+            }
+            P.N[d] = in.iupper[d] - in.ilower[d] + 1;
+            if (P.N[d] > 30000) return IBX_E_TOO_LARGE; // stencil bases are stored as int16
+            P.ntile[d] = (P.N[d] + E - 1) / E;
+            ntiles *= P.ntile[d];
+            vol *= P.N[d];
+            P.dx[d] = chk.dx[d];
+            P.inv_dx[d] = chk.inv_dx[d];
+            P.dx_pow2[d] = chk.dx_pow2[d];
+            // Positions are measured from the box origin: index ilower sits at
+            // x_lower, so the stencil bases come out relative to ilower.
+            P.xlo_c[d] = in.x_lower[d];
+            P.xlo_s[d] = in.x_lower[d] - 0.5 * in.dx[d];
+            if (!fixed_dim(in.x_lower[d], in.x_upper[d], in.dx[d], P.fx[d])) P.fixed_ok = -1;
+            const int bound = P.ntile[d] < 2 + (P.N[d] % E != 0) ? P.ntile[d] : 2 + (P.N[d] % E != 0);
+            per *= bound;
+        }
+        const ibx_problem& ii = interp_problems[p];
+        if (&ii != &in)
+        {
+            // Same geometry and markers; only the data arrays may differ.
+            Prob chk2;
+            const int rc2 = build_prob(ii, kernel, false, chk2);
+            if (rc2) return rc2;
+            bool same = ii.dim == in.dim && ii.centering == in.centering && ii.mode == in.mode && ii.X == in.X &&
+                        ii.n_markers == in.n_markers && ii.Q_depth == in.Q_depth && ii.q_depth == in.q_depth &&
+                        !ii.indices && !ii.Xshift;
+            for (int d = 0; d < dim; ++d)
+                same = same && ii.ilower[d] == in.ilower[d] && ii.iupper[d] == in.iupper[d] &&
+                       ii.dx[d] == in.dx[d] && ii.x_lower[d] == in.x_lower[d];
+            if (!same) return IBX_E_ARG;
+        }
+        P.fixed_ok = P.fixed_ok < 0 ? 0 : 1;
+        P.inv_vol = (float)(1.0 / chk.vol);
+        P.X = in.X;
+        P.Q = in.Q;
+        P.Qi = ii.Q;
+        for (int c = 0; c < ncomp; ++c)
+        {
+            P.q[c] = P.side ? in.q[c] : static_cast<void*>(static_cast<float*>(in.q[0]) + vol * c);
+            P.qi[c] = P.side ? ii.q[c] : static_cast<void*>(static_cast<float*>(ii.q[0]) + vol * c);
+        }
+        P.tile0 = toffs[p];
+        P.marker0 = moffs[p];
+        if ((long long)toffs[p] + ntiles > 0x3fffffffLL) return IBX_E_TOO_LARGE;
+        toffs[p + 1] = toffs[p] + (int)ntiles;
+        moffs[p + 1] = moffs[p] + in.n_markers;
+        visit_cap += (long long)in.n_markers * per;
+    }
+    if (moffs[n_problems] > 0x7fffffffLL) return IBX_E_TOO_LARGE;
+    const int item_visits = item_visits_setting();
+    const long long item_cap = toffs[n_problems] + visit_cap / item_visits + 1;
+    if (item_cap > 0x7fffffffLL || visit_cap > 0x7fffffffLL) return IBX_E_TOO_LARGE;
+    ibx_plan* plan = new (std::nothrow) ibx_plan;
+    if (!plan) return IBX_E_OOM;
+    std::memset(plan, 0, sizeof(*plan));
+    plan->dim = dim;
+    plan->kernel = kernel;
+    plan->precision = precision;
+    plan->n_probs = n_problems;
+    plan->max_ncomp = max_ncomp;
+    const long long nm = moffs[n_problems];
+    const int nt = toffs[n_problems];
+    // One device allocation holds every buffer of the plan.
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const size_t o_probs = take(sizeof(PlanProb) * n_problems);
+    const size_t o_moffs = take(sizeof(long long) * (n_problems + 1));
+    const size_t o_toffs = take(sizeof(int) * (n_problems + 1));
+    const size_t o_rec = take(sizeof(Rec) * nm);
+    const size_t o_home_tile = take(sizeof(int) * nm);
+    // hcount, vcount (+1 each), both cursors, items (+1): zeroed together every step
+    const size_t o_counts = take(sizeof(int) * (5 * (size_t)nt + 3));
+    const size_t o_item_tile = take(sizeof(int) * item_cap);
+    const size_t o_home_list = take(sizeof(int) * nm);
+    const size_t o_visit = take(sizeof(int) * visit_cap);
+    const size_t o_status = take(sizeof(int) * 4);
+    const size_t o_scan = take(sizeof(int) * 2048);
+    void* dmem = nullptr;
+    if (cudaMalloc(&dmem, off) != cudaSuccess)
+    {
+        delete plan;
+        return IBX_E_OOM;
+    }
+    char* b = static_cast<char*>(dmem);
+    if (cudaMemcpy(b + o_probs, hp.data(), sizeof(PlanProb) * n_problems, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b + o_moffs, moffs.data(), sizeof(long long) * (n_problems + 1), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(b + o_toffs, toffs.data(), sizeof(int) * (n_problems + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(b + o_status, 0, sizeof(int) * 4) != cudaSuccess)
+    {
+        cudaFree(dmem);
+        delete plan;
+        return IBX_E_CUDA;
+    }
+    DevPlan& D = plan->D;
+    D.probs = reinterpret_cast<const PlanProb*>(b + o_probs);
+    D.marker_offs = reinterpret_cast<const long long*>(b + o_moffs);
+    D.tile_offs = reinterpret_cast<const int*>(b + o_toffs);
+    D.n_probs = n_problems;
+    D.n_markers = nm;
+    D.n_tiles = nt;
+    D.rec = reinterpret_cast<Rec*>(b + o_rec);
+    D.home_tile = reinterpret_cast<int*>(b + o_home_tile);
+    int* counts = reinterpret_cast<int*>(b + o_counts);
+    D.hcount = counts;
+    D.vcount = counts + (nt + 1);
+    D.hcursor = counts + 2 * (nt + 1);
+    D.vcursor = counts + 2 * (nt + 1) + nt;
+    D.items = counts + 2 * (nt + 1) + 2 * nt;
+    D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
+    D.n_item_cap = (int)item_cap;
+    D.item_visits = item_visits;
+    D.home_list = reinterpret_cast<int*>(b + o_home_list);
+    D.visit_list = reinterpret_cast<int*>(b + o_visit);
+    D.n_visit_cap = visit_cap;
+    D.status = reinterpret_cast<int*>(b + o_status);
+    plan->scan_tmp = reinterpret_cast<int*>(b + o_scan);
+    plan->dmem = dmem;
+    plan->dbytes = off;
+    *out = plan;
+    return IBX_OK;
+}
+
+int
+ibx_plan_bin(ibx_plan* plan, void* stream)
+{
+    using namespace ibx;
+    if (!plan) return IBX_E_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DevPlan& D = plan->D;
+    const int nt = D.n_tiles;
+    // Counters, cursors and item counts are contiguous: one memset.
+    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * (5 * (size_t)nt + 3), s) != cudaSuccess) return IBX_E_CUDA;
+    int rc = launch_bin(plan->dim, plan->kernel, D, s, false);
+    if (!rc) rc = exclusive_scan(D.hcount, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = launch_bin(plan->dim, plan->kernel, D, s, true);
+    if (!rc) rc = launch_items(D, s);
+    if (!rc) rc = exclusive_scan(D.items, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = launch_items_fill(D, s);
+    return rc;
+}
+
+int
+ibx_plan_spread(ibx_plan* plan, void* stream)
+{
+    if (!plan) return IBX_E_ARG;
+    return ibx::launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, static_cast<cudaStream_t>(stream));
+}
+
+int
+ibx_plan_interpolate(ibx_plan* plan, void* stream)
+{
+    if (!plan) return IBX_E_ARG;
+    return ibx::launch_interp(plan->dim, plan->kernel, plan->D, static_cast<cudaStream_t>(stream));
+}
+
+int
+ibx_plan_get_bins(const ibx_plan* plan, int* base_c, int* base_s, int* home_tile, int* tile_start, int* home_list)
+{
+    using namespace ibx;
+    if (!plan) return IBX_E_ARG;
+    if (cudaDeviceSynchronize() != cudaSuccess) return IBX_E_CUDA;
+    const DevPlan& D = plan->D;
+    const long long nm = D.n_markers;
+    if (base_c || base_s)
+    {
+        std::vector<Rec> rec(nm);
+        if (nm && cudaMemcpy(rec.data(), D.rec, sizeof(Rec) * nm, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return IBX_E_CUDA;
+        for (long long g = 0; g < nm; ++g)
+            for (int d = 0; d < 3; ++d)
+            {
+                if (base_c) base_c[3 * g + d] = rec[g].bc[d];
+                if (base_s) base_s[3 * g + d] = rec[g].bs[d];
+            }
+    }
+    if (home_tile && nm && cudaMemcpy(home_tile, D.home_tile, sizeof(int) * nm, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return IBX_E_CUDA;
+    if (tile_start &&
+        cudaMemcpy(tile_start, D.hcount, sizeof(int) * (D.n_tiles + 1), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return IBX_E_CUDA;
+    if (home_list && nm && cudaMemcpy(home_list, D.home_list, sizeof(int) * nm, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return IBX_E_CUDA;
+    return IBX_OK;
+}
+
+int
+ibx_plan_status(ibx_plan* plan, void* stream, int* status)
+{
+    using namespace ibx;
+    if (!plan || !status) return IBX_E_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int word = 0;
+    if (cudaMemcpyAsync(&word, plan->D.status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess || cudaMemsetAsync(plan->D.status, 0, sizeof(int), s) != cudaSuccess)
+        return IBX_E_CUDA;
+    *status = (word & 1) ? IBX_E_NONFINITE : (word & 2) ? IBX_E_TOO_LARGE : IBX_OK;
+    return IBX_OK;
+}
+
+int
+ibx_plan_n_tiles(const ibx_plan* plan)
+{
+    return plan ? plan->D.n_tiles : -1;
+}
+
+long long
+ibx_plan_scratch_bytes(const ibx_plan* plan)
+{
+    return plan ? (long long)plan->dbytes : 0;
+}
+
+int
+ibx_plan_destroy(ibx_plan* plan)
+{
+    if (!plan) return IBX_OK;
+    const cudaError_t e = cudaFree(plan->dmem);
+    delete plan;
+    return e == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+} // extern "C"

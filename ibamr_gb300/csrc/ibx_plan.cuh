@@ -1,0 +1,196 @@
+// ibx_plan.cuh -- data structures and device helpers of the binned plan
+// pipeline (bin -> scan -> scatter -> spread / interpolate).
+#pragma once
+
+#include "ibx_internal.h"
+
+namespace ibx
+{
+constexpr int TILE3 = 8;  // tile edge in 3D (cells)
+constexpr int TILE2 = 16; // tile edge in 2D
+
+template <int DIM>
+struct TileT
+{
+    static constexpr int E = DIM == 3 ? TILE3 : TILE2;
+    static constexpr int PTS = DIM == 3 ? E * E * E : E * E;
+};
+
+// Per-marker stencil record (32 bytes).  For every dimension: the stencil
+// base (relative to the box's lower index, shifted by a multiple of N into
+// [0, N) for the cell-centred one) of the cell-centred and of the staggered
+// (side-normal) position, and r_first = t - (base + 1/2), the distance in
+// cells of the marker from the first stencil point, computed exactly and
+// rounded once to FP32.
+struct __align__(16) Rec
+{
+    float rc[3];
+    float rs[3];
+    short bc[3];
+    short bs[3];
+};
+
+// Exact fixed-point description of t = (X - x_lower)/dx for one dimension
+// (see ibx_bin.cu): Xf = floor(X*2^sx), D = Xf - xlo_f, T = mulhi(D, inv_f),
+// t = T / 2^F up to 2^-40 cells.
+struct FixedDim
+{
+    long long xlo_c_f, xlo_s_f; // x_lower and x_lower - dx/2 in units of 2^-sx
+    long long inv_f;            // 1/dx in units of 2^-si
+    int sx, F;                  // F = sx + si - 64
+    int dshift;                 // decision margin: 2^dshift units of 2^-F
+};
+
+// Per-problem data (device side).
+struct PlanProb
+{
+    int dim, ncomp, side, Q_depth;
+    int N[3];          // cells per dim
+    int ntile[3];      // tiles per dim
+    int tile0;         // first global tile id of this problem
+    long long marker0; // first global marker id of this problem
+    double dx[3], inv_dx[3];
+    double xlo_c[3], xlo_s[3];
+    int dx_pow2[3];
+    int fixed_ok;      // the fixed-point index path is valid for this problem
+    FixedDim fx[3];
+    float inv_vol;     // 1/(dx0*dx1[*dx2]) rounded to FP32
+    const double* X;
+    void* Q;           // spread source
+    void* q[3];        // spread target, one array per component (side axis or cell depth)
+    void* Qi;          // interpolation target
+    void* qi[3];       // interpolation source
+};
+
+struct DevPlan
+{
+    const PlanProb* probs;
+    const long long* marker_offs; // [n_probs+1]
+    const int* tile_offs;         // [n_probs+1]
+    int n_probs;
+    long long n_markers;
+    int n_tiles;
+    Rec* rec;         // [n_markers], original marker order
+    int* home_tile;   // [n_markers]
+    int* hcount;      // [n_tiles+1], scanned in place into start offsets
+    int* vcount;      // [n_tiles+1]
+    int* hcursor;     // [n_tiles]
+    int* vcursor;     // [n_tiles]
+    int* home_list;   // [n_markers] global marker ids grouped by home tile
+    int* visit_list;  // [n_visit_cap] global marker ids grouped by visited tile
+    long long n_visit_cap;
+    int* items;       // [n_tiles+1] spread work items per tile, scanned into offsets
+    int* item_tile;   // [n_item_cap] tile of each work item
+    int n_item_cap;
+    int item_visits;  // visits per spread work item
+    int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
+};
+
+template <typename T>
+__device__ __forceinline__ int
+find_in_offsets(const T* offs, int n, T g)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (offs[mid] <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int
+wrap_cell(int c, int N)
+{
+    while (c >= N) c -= N;
+    while (c < 0) c += N;
+    return c;
+}
+
+// ---- FP32 weights (mixed form) --------------------------------------------
+__device__ __forceinline__ float
+pcubic_f(float r)
+{
+    r = fabsf(r);
+    if (r < 1.f) return 1.f - 0.5f * r - r * r + 0.5f * r * r * r;
+    if (r < 2.f) return 1.f - (11.f / 6.f) * r + r * r - (1.f / 6.f) * r * r * r;
+    return 0.f;
+}
+__device__ __forceinline__ float
+ib3_f(float r)
+{
+    r = fabsf(r);
+    if (r < 0.5f) return 0.333333333333333f * (1.f + sqrtf(1.f - 3.f * r * r));
+    if (r < 1.5f) return 0.16666666666667f * (5.f - 3.f * r - sqrtf(1.f - 3.f * (1.f - r) * (1.f - r)));
+    return 0.f;
+}
+__device__ __forceinline__ float
+bspline4_f(float x)
+{
+    const float modx = fabsf(x);
+    const float r = modx + 2.f;
+    const float r2 = r * r;
+    const float r3 = r2 * r;
+    if (modx <= 1.f) return (1.f / 6.f) * (3.f * r3 - 24.f * r2 + 60.f * r - 44.f);
+    if (modx <= 2.f) return (1.f / 6.f) * (-r3 + 12.f * r2 - 48.f * r + 64.f);
+    return 0.f;
+}
+
+// The W weights of one dimension from r_first; the formulas of the FP64
+// path (ibx_device.cuh) evaluated in FP32.
+template <int K>
+__device__ __forceinline__ void
+weights_f32(float rf, float* w)
+{
+    if (K == K_IB4)
+    {
+        const float r = rf - 1.f;
+        const float q = sqrtf(1.f + 4.f * r * (1.f - r));
+        w[0] = 0.125f * (3.f - 2.f * r - q);
+        w[1] = 0.125f * (3.f - 2.f * r + q);
+        w[2] = 0.125f * (1.f + 2.f * r + q);
+        w[3] = 0.125f * (1.f + 2.f * r - q);
+    }
+    else if (K == K_IB6)
+        ib6_weights<float>(3.f - rf, w);
+    else if (K == K_PL)
+    {
+        w[0] = 1.f - rf;
+        w[1] = rf;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < KT<K>::W; ++i)
+        {
+            const float a = rf - (float)i;
+            w[i] = (K == K_IB3) ? ib3_f(a) : (K == K_PCUBIC) ? pcubic_f(a) : bspline4_f(a);
+        }
+    }
+}
+
+// Compensated accumulation into shared memory: the FP32 atomic returns the
+// previous value, so the exact rounding error of the stored sum follows from
+// Knuth's TwoSum and is accumulated into the low word (double-FP32 sum).
+__device__ __forceinline__ void
+acc2(float* hi, float* lo, float v)
+{
+    const float old = atomicAdd(hi, v);
+    const float s = old + v;
+    const float bp = s - old;
+    const float err = (old - (s - bp)) + (v - bp);
+    if (err != 0.f) atomicAdd(lo, err);
+}
+
+// Launchers (ibx_bin.cu, ibx_spread.cu, ibx_interp.cu).
+int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter);
+int exclusive_scan(int* data, int n, int* tmp, cudaStream_t s);
+int launch_items(const DevPlan& D, cudaStream_t s);
+int launch_items_fill(const DevPlan& D, cudaStream_t s);
+int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
+int launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s);
+
+} // namespace ibx

@@ -1,0 +1,248 @@
+"""Python binding of libibx (include/ibx.h) over ctypes.
+
+This is host plumbing for tests, benchmarks and Python users: device memory
+comes from torch tensors, calls go straight to the C ABI.  There is no CPU
+fallback: importing works without a GPU, but every compute call needs the
+CUDA library and a device, and raises otherwise.
+"""
+
+import ctypes
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libibx.so")
+
+PIECEWISE_LINEAR, PIECEWISE_CUBIC, IB_3, IB_4, IB_6, BSPLINE_4 = range(6)
+KERNELS = {"PIECEWISE_LINEAR": 0, "PIECEWISE_CUBIC": 1, "IB_3": 2, "IB_4": 3, "IB_6": 4, "BSPLINE_4": 5}
+FP64, MIXED = 0, 1
+CELL, SIDE = 0, 1
+MODE_PATCH, MODE_PERIODIC = 0, 1
+
+OK = 0
+E_BAD_KERNEL, E_GHOST_WIDTH, E_DEPTH, E_ARG, E_CUDA, E_OOM, E_TIMEOUT, E_NONFINITE, E_TOO_LARGE = range(1, 10)
+
+
+class IbxError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        super().__init__("%s: %s (status %d)" % (where or "libibx", status_string(status), status))
+
+
+class Problem(ctypes.Structure):
+    """ibx_problem (include/ibx.h)."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int), ("centering", ctypes.c_int), ("mode", ctypes.c_int),
+        ("ilower", ctypes.c_int * 3), ("iupper", ctypes.c_int * 3), ("gcw", ctypes.c_int * 3),
+        ("dx", ctypes.c_double * 3), ("x_lower", ctypes.c_double * 3), ("x_upper", ctypes.c_double * 3),
+        ("touches_physical_lower", ctypes.c_int * 3), ("touches_physical_upper", ctypes.c_int * 3),
+        ("q_depth", ctypes.c_int), ("q", ctypes.c_void_p * 3),
+        ("X", ctypes.c_void_p), ("Q", ctypes.c_void_p), ("Q_depth", ctypes.c_int),
+        ("n_markers", ctypes.c_int), ("indices", ctypes.c_void_p), ("n_indices", ctypes.c_int),
+        ("Xshift", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libibx.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libibx.so is missing (%s): build it with python -m ibamr_gb300.build" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER(Problem)
+        L.ibx_get_stencil_size.argtypes = [ctypes.c_int]
+        L.ibx_get_minimum_ghost_width.argtypes = [ctypes.c_int]
+        L.ibx_kernel_from_name.argtypes = [ctypes.c_char_p]
+        L.ibx_status_string.argtypes = [ctypes.c_int]
+        L.ibx_status_string.restype = ctypes.c_char_p
+        for name in ("ibx_interpolate", "ibx_spread"):
+            getattr(L, name).argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        if hasattr(L, "ibx_plan_create"):
+            L.ibx_plan_create.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_void_p)]
+            L.ibx_plan_create2.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]
+            for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate"):
+                getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
+            L.ibx_plan_scratch_bytes.restype = ctypes.c_longlong
+            L.ibx_plan_destroy.argtypes = [ctypes.c_void_p]
+            ip = ctypes.POINTER(ctypes.c_int)
+            L.ibx_plan_get_bins.argtypes = [ctypes.c_void_p, ip, ip, ip, ip, ip]
+            L.ibx_plan_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ip]
+            L.ibx_plan_n_tiles.argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def status_string(status):
+    try:
+        return lib().ibx_status_string(int(status)).decode()
+    except Exception:  # library missing
+        return "status %d" % status
+
+
+def kernel_id(kernel):
+    if isinstance(kernel, str):
+        k = lib().ibx_kernel_from_name(kernel.encode())
+        if k < 0:
+            raise IbxError(E_BAD_KERNEL, "unknown kernel %r" % kernel)
+        return k
+    return int(kernel)
+
+
+def get_stencil_size(kernel):
+    return lib().ibx_get_stencil_size(kernel_id(kernel))
+
+
+def get_minimum_ghost_width(kernel):
+    return lib().ibx_get_minimum_ghost_width(kernel_id(kernel))
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+def make_problem(dim, centering, mode, ilower, iupper, dx, x_lower, x_upper, q, X, Q, Q_depth=None, q_depth=1,
+                 gcw=(0, 0, 0), indices=None, Xshift=None, touches_physical_lower=(0, 0, 0),
+                 touches_physical_upper=(0, 0, 0), n_markers=None):
+    """Build an ibx_problem from torch tensors (device memory).  ``q`` is a
+    tensor (cell data) or a list of one tensor per axis (side data)."""
+    P = Problem()
+    P.dim = dim
+    P.centering = centering
+    P.mode = mode
+    for d in range(3):
+        P.ilower[d] = int(ilower[d]) if d < dim else 0
+        P.iupper[d] = int(iupper[d]) if d < dim else 0
+        P.gcw[d] = int(gcw[d]) if d < len(gcw) else 0
+        P.dx[d] = float(dx[d]) if d < dim else 1.0
+        P.x_lower[d] = float(x_lower[d]) if d < dim else 0.0
+        P.x_upper[d] = float(x_upper[d]) if d < dim else 1.0
+        P.touches_physical_lower[d] = int(touches_physical_lower[d]) if d < len(touches_physical_lower) else 0
+        P.touches_physical_upper[d] = int(touches_physical_upper[d]) if d < len(touches_physical_upper) else 0
+    qs = q if isinstance(q, (list, tuple)) else [q]
+    for a, t in enumerate(qs):
+        P.q[a] = t.data_ptr()
+    P.q_depth = q_depth
+    P.X = X.data_ptr()
+    P.Q = Q.data_ptr()
+    P.Q_depth = Q_depth if Q_depth is not None else (dim if centering == SIDE else q_depth)
+    P.n_markers = int(n_markers if n_markers is not None else X.numel() // dim)
+    if indices is not None:
+        P.indices = indices.data_ptr()
+        P.n_indices = int(indices.numel())
+    if Xshift is not None:
+        P.Xshift = Xshift.data_ptr()
+    P._keep = (qs, X, Q, indices, Xshift)  # keep tensors alive with the descriptor
+    return P
+
+
+def _array(problems):
+    if isinstance(problems, Problem):
+        problems = [problems]
+    arr = (Problem * len(problems))(*problems)
+    return arr, len(problems)
+
+
+def spread(problems, kernel, precision=FP64, stream=None):
+    arr, n = _array(problems)
+    rc = lib().ibx_spread(arr, n, kernel_id(kernel), precision, _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_spread")
+
+
+def interpolate(problems, kernel, precision=FP64, stream=None):
+    arr, n = _array(problems)
+    rc = lib().ibx_interpolate(arr, n, kernel_id(kernel), precision, _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_interpolate")
+
+
+class Plan:
+    """Binned spread/interpolate pipeline over fixed IBX_MODE_PERIODIC problems."""
+
+    def __init__(self, problems, kernel, precision=MIXED, interp_problems=None):
+        arr, n = _array(problems)
+        self._problems = (problems, interp_problems)
+        self._arr = arr
+        h = ctypes.c_void_p()
+        if interp_problems is None:
+            rc = lib().ibx_plan_create(arr, n, kernel_id(kernel), precision, ctypes.byref(h))
+        else:
+            arr2, n2 = _array(interp_problems)
+            self._arr2 = arr2
+            if n2 != n:
+                raise IbxError(E_ARG, "ibx_plan_create2")
+            rc = lib().ibx_plan_create2(arr, arr2, n, kernel_id(kernel), precision, ctypes.byref(h))
+        if rc:
+            raise IbxError(rc, "ibx_plan_create")
+        self.h = h
+
+    def bin(self, stream=None):
+        rc = lib().ibx_plan_bin(self.h, _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_plan_bin")
+
+    def spread(self, stream=None):
+        rc = lib().ibx_plan_spread(self.h, _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_plan_spread")
+
+    def interpolate(self, stream=None):
+        rc = lib().ibx_plan_interpolate(self.h, _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_plan_interpolate")
+
+    def status(self, stream=None):
+        st = ctypes.c_int(0)
+        rc = lib().ibx_plan_status(self.h, _stream_handle(stream), ctypes.byref(st))
+        if rc:
+            raise IbxError(rc, "ibx_plan_status")
+        return st.value
+
+    @property
+    def n_tiles(self):
+        return lib().ibx_plan_n_tiles(self.h)
+
+    def bins(self, n_markers):
+        """(base_c, base_s, home_tile, tile_start, home_list) as numpy arrays."""
+        import numpy as np
+
+        ip = ctypes.POINTER(ctypes.c_int)
+        bc = np.zeros(3 * n_markers, dtype=np.int32)
+        bs = np.zeros(3 * n_markers, dtype=np.int32)
+        ht = np.zeros(n_markers, dtype=np.int32)
+        ts = np.zeros(self.n_tiles + 1, dtype=np.int32)
+        hl = np.zeros(n_markers, dtype=np.int32)
+        rc = lib().ibx_plan_get_bins(self.h, *(a.ctypes.data_as(ip) for a in (bc, bs, ht, ts, hl)))
+        if rc:
+            raise IbxError(rc, "ibx_plan_get_bins")
+        return bc, bs, ht, ts, hl
+
+    @property
+    def scratch_bytes(self):
+        return lib().ibx_plan_scratch_bytes(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ibx_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,179 @@
+/*
+ * ibx.h -- C ABI of the GB300 Lagrangian-Eulerian interaction library
+ * (libibx.so).  Spreading of marker values onto staggered (side-centred) or
+ * cell-centred grids and interpolation of grid values onto markers with the
+ * regularized delta kernels of IBAMR's IBTK::LEInteractor.
+ *
+ * Every entry point is stream-ordered, reentrant and returns a status code
+ * instead of aborting.  Pointers inside ibx_problem are DEVICE pointers
+ * unless stated otherwise.  Nothing here allocates memory on the caller's
+ * behalf except ibx_plan_create (see there).
+ *
+ * Reference interfaces replaced (paths inside the IBAMR tree):
+ *   LEI.h  = ibtk/include/ibtk/LEInteractor.h
+ *   LEI    = ibtk/src/lagrangian/LEInteractor.cpp
+ */
+#ifndef IBX_H
+#define IBX_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- kernels (LEI:1923-2016 string_to_kernel) ------------------------- */
+enum
+{
+    IBX_KERNEL_PIECEWISE_LINEAR = 0,
+    IBX_KERNEL_PIECEWISE_CUBIC = 1,
+    IBX_KERNEL_IB_3 = 2,
+    IBX_KERNEL_IB_4 = 3,
+    IBX_KERNEL_IB_6 = 4,
+    IBX_KERNEL_BSPLINE_4 = 5
+};
+
+/* ---- precision forms -------------------------------------------------- */
+enum
+{
+    /* FP64 everywhere: grid values, marker values, weights, accumulation. */
+    IBX_PRECISION_FP64 = 0,
+    /* Grid and marker values stored and multiplied in FP32; positions,
+     * stencil indices and kernel arguments in FP64; spread sums accumulated
+     * in a double-FP32 (compensated, ~48-bit) accumulator. */
+    IBX_PRECISION_MIXED = 1
+};
+
+/* ---- data centering --------------------------------------------------- */
+enum
+{
+    IBX_CELL = 0, /* SAMRAI CellData: one array of q_depth components */
+    IBX_SIDE = 1  /* SAMRAI SideData: one array per axis, on toSideBox(box, axis) */
+};
+
+/* ---- problem modes ---------------------------------------------------- */
+enum
+{
+    /* Reference semantics of one LEInteractor call on one patch: markers
+     * selected by indices (+ periodic shifts Xshift), stencils clipped to
+     * the ghost box, arrays in SAMRAI layout (ghosts included, Fortran
+     * order, depth slowest).  Ghost values are written by spreading. */
+    IBX_MODE_PATCH = 0,
+    /* One patch that covers a periodic domain, stored compactly: each
+     * component is N0 x N1 (x N2) values, x fastest, no ghosts, and side
+     * arrays hold N faces along their normal (face N is face 0).  Stencil
+     * indices wrap modulo N, so no periodic image markers are needed. */
+    IBX_MODE_PERIODIC = 1
+};
+
+/* ---- status codes ----------------------------------------------------- */
+enum
+{
+    IBX_OK = 0,
+    IBX_E_BAD_KERNEL = 1,  /* unknown kernel id or name (LEI:2014) */
+    IBX_E_GHOST_WIDTH = 2, /* ghost width below getMinimumGhostWidth (LEI:4488-4498, 5250-5268) */
+    IBX_E_DEPTH = 3,       /* Q_depth / q_depth mismatch (LEI:2197-2201, 3650-3654) */
+    IBX_E_ARG = 4,         /* malformed argument (null pointer, bad dim, bad sizes) */
+    IBX_E_CUDA = 5,        /* a CUDA runtime call failed */
+    IBX_E_OOM = 6,         /* device memory exhausted */
+    IBX_E_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+    IBX_E_NONFINITE = 8,   /* a marker position is NaN or infinite */
+    IBX_E_TOO_LARGE = 9    /* a size exceeds a documented limit */
+};
+
+/* One patch-level interaction problem: the arguments of the reference's
+ * private LEInteractor::interpolate / spread (LEI.h:1326-1361) with device
+ * pointers.  Several problems can be passed in one call; they run in one
+ * launch and must not share output memory. */
+typedef struct ibx_problem
+{
+    int dim;       /* 2 or 3 */
+    int centering; /* IBX_CELL or IBX_SIDE */
+    int mode;      /* IBX_MODE_PATCH or IBX_MODE_PERIODIC */
+    int ilower[3]; /* patch cell box (Patch::getBox()) */
+    int iupper[3];
+    int gcw[3];    /* ghost cell width of the Eulerian data (IBX_MODE_PATCH) */
+    double dx[3];  /* CartesianPatchGeometry::getDx/getXLower/getXUpper */
+    double x_lower[3];
+    double x_upper[3];
+    int touches_physical_lower[3]; /* getTouchesRegularBoundary(axis, 0/1) */
+    int touches_physical_upper[3];
+    int q_depth;        /* CellData depth; SideData requires 1 */
+    void* q[3];         /* cell: q[0]; side: q[axis].  double or float */
+    const double* X;    /* X[dim*s + d], FP64 */
+    void* Q;            /* Q[Q_depth*s + k]; double (FP64) or float (MIXED) */
+    int Q_depth;        /* cell: == q_depth; side: == dim */
+    int n_markers;      /* marker slots addressed by s */
+    const int* indices; /* IBX_MODE_PATCH: local marker indices, or NULL = 0..n_markers-1 */
+    int n_indices;      /* entries of indices (ignored when indices is NULL) */
+    const double* Xshift; /* IBX_MODE_PATCH: dim shifts per index entry, or NULL = 0 */
+} ibx_problem;
+
+/* LEInteractor::getStencilSize (LEI:2052-2108); -1 for an unknown kernel. */
+int ibx_get_stencil_size(int kernel);
+/* LEInteractor::getMinimumGhostWidth (LEI:2110-2114); -1 for an unknown kernel. */
+int ibx_get_minimum_ghost_width(int kernel);
+/* LEInteractor::isKnownKernel + string_to_kernel (LEI:1923-2050) restricted
+ * to the kernels this library implements; -1 for any other name. */
+int ibx_kernel_from_name(const char* name);
+/* Human-readable text of a status code. */
+const char* ibx_status_string(int status);
+
+/* LEInteractor::interpolate (LEI:2186-2489, 2804-2862, 3044-3127 and the
+ * private form LEI:4470-5230): overwrite Q at the selected markers with the
+ * kernel-weighted sum of q.  Markers not selected are left untouched.
+ * Direct marker-parallel form without scratch memory; with n_problems > 1
+ * the descriptor table is staged in stream-ordered device memory
+ * (cudaMallocAsync) and the call synchronises the stream. */
+int ibx_interpolate(const ibx_problem* problems, int n_problems, int kernel, int precision, void* stream);
+
+/* LEInteractor::spread (LEI:3341-3714, 3950-4264 and the private form
+ * LEI:5232-6006): q += kernel-weighted Q / prod(dx) for the selected
+ * markers.  Direct marker-parallel form using FP64 device atomics, no
+ * scratch memory; n_problems > 1 as for ibx_interpolate. */
+int ibx_spread(const ibx_problem* problems, int n_problems, int kernel, int precision, void* stream);
+
+/* ---- binned plans (the fast path) ------------------------------------- */
+/* A plan owns the scratch memory of the binned spread/interpolate pipeline
+ * for a fixed set of IBX_MODE_PERIODIC problems (grids, marker arrays and
+ * capacities fixed at creation; positions and values may change between
+ * steps).  ibx_plan_bin sorts the markers of every problem by grid tile
+ * (integer counting sort) and derives their stencil indices and kernel
+ * arguments in FP64; ibx_plan_spread / ibx_plan_interpolate then run one
+ * launch each over all problems.  All three are CUDA-graph capturable once
+ * the plan exists.  ibx_plan_create allocates device memory (the only entry
+ * point that does). */
+typedef struct ibx_plan ibx_plan;
+
+int ibx_plan_create(const ibx_problem* problems, int n_problems, int kernel, int precision, ibx_plan** plan);
+/* As ibx_plan_create, with separate data for interpolation: spreading
+ * reads Q and adds into q of `problems`, interpolation reads q and writes Q
+ * of `interp_problems`.  Both arrays must describe the same geometry and the
+ * same marker positions X (one binning serves both). */
+int ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
+                     int precision, ibx_plan** plan);
+int ibx_plan_bin(ibx_plan* plan, void* stream);
+int ibx_plan_spread(ibx_plan* plan, void* stream);
+int ibx_plan_interpolate(ibx_plan* plan, void* stream);
+/* Status of the marker data seen by the last ibx_plan_bin (synchronises
+ * the stream, then clears the word): IBX_OK, IBX_E_NONFINITE (a position
+ * was NaN or infinite; that marker was skipped) or IBX_E_TOO_LARGE. */
+int ibx_plan_status(ibx_plan* plan, void* stream, int* status);
+/* Copy the binning of the last ibx_plan_bin to host arrays (any may be
+ * NULL; synchronises the device).  Markers are numbered across problems in
+ * order.  base_c / base_s: 3 ints per marker, the stencil base index of the
+ * cell-centred and of the staggered position per dimension, relative to
+ * ilower and shifted by a multiple of N into [0, N) (base_c); home_tile: the
+ * tile owning the marker; tile_start: n_tiles+1 offsets of each tile's
+ * markers in home_list. */
+int ibx_plan_get_bins(const ibx_plan* plan, int* base_c, int* base_s, int* home_tile, int* tile_start,
+                      int* home_list);
+/* Number of tiles of the plan (all problems). */
+int ibx_plan_n_tiles(const ibx_plan* plan);
+/* Bytes of device scratch the plan holds. */
+long long ibx_plan_scratch_bytes(const ibx_plan* plan);
+int ibx_plan_destroy(ibx_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IBX_H */

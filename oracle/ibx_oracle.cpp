@@ -449,6 +449,20 @@ ibxo_nint(double a)
 }
 
 int
+ibxo_stencil_1d(int kernel, double X, double Xshift, double x_lower, double dx, int ilower, int iupper, int ghost,
+                int* base, int* start, int* stop, double* w)
+{
+    if (!valid_kernel(kernel)) return IBXO_E_BAD_KERNEL;
+    Sten S;
+    stencil_1d(kernel, X, Xshift, x_lower, dx, ilower, iupper, ghost, S);
+    *base = S.base;
+    *start = S.start;
+    *stop = S.stop;
+    for (int i = 0; i < 6; ++i) w[i] = i <= S.stop ? S.w[i] : 0.0;
+    return IBXO_OK;
+}
+
+int
 ibxo_fortran_interp(int kernel, int dim, const double* dx, const double* x_lower, const double* /*x_upper*/,
                     int depth, const int* ilower, const int* iupper, const int* nugc, const double* u,
                     const int* indices, const double* Xshift, int nindices, const double* X, double* V)
@@ -518,12 +532,11 @@ ibxo_cache_local_indices(const ibxo_patch* P, const int* periodic_shift, const i
         const int nimg = dim == 2 ? 9 : 27;
         for (int m = 0; m < nimg; ++m)
         {
-            int k[3] = { m % 3 - 1, (m / 3) % 3 - 1, (m / 9) % 3 - 1 };
+            const int k[3] = { m % 3 - 1, (m / 3) % 3 - 1, dim == 3 ? (m / 9) % 3 - 1 : 0 };
             bool ok = true;
             int off[3] = { 0, 0, 0 };
             for (int d = 0; d < dim && ok; ++d)
             {
-                if (dim == 2 && d == 2) break;
                 const int i = c[d] + k[d] * periodic_shift[d];
                 if (k[d] != 0 && periodic_shift[d] == 0) ok = false;
                 if (i < lo[d] || i > hi[d]) ok = false;
@@ -537,7 +550,6 @@ ibxo_cache_local_indices(const ibxo_patch* P, const int* periodic_shift, const i
                     off[d] = 0;
                 if (off[d] != k[d] * periodic_shift[d]) ok = false;
             }
-            if (dim == 2 && k[2] != 0) ok = false;
             if (!ok) continue;
             if (n < capacity)
             {
@@ -869,9 +881,9 @@ ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const dou
     for (int d = 0; d < 3; ++d) plan->N[d] = d < dim ? N[d] : 1;
     const int split = dim - 1;
     n_patches = std::min(n_patches, plan->N[split]);
-    for (int p = 0; p < n_patches; ++p)
-    {
-        CpuPatch cp;
+    plan->patches.resize(n_patches);
+    auto build_patch = [plan, dim, split, n_patches, n_markers, X](int p) {
+        CpuPatch& cp = plan->patches[p];
         ibxo_patch& P = cp.P;
         std::memset(&P, 0, sizeof(P));
         P.dim = dim;
@@ -914,8 +926,12 @@ ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const dou
             cp.f_loc[a].assign(vol, 0.0);
             cp.u_loc[a].assign(vol, 0.0);
         }
-        plan->patches.push_back(std::move(cp));
-    }
+    };
+    // Patches are independent: build their index sets concurrently.
+    std::vector<std::thread> threads;
+    for (int p = 1; p < n_patches; ++p) threads.emplace_back(build_patch, p);
+    build_patch(0);
+    for (auto& t : threads) t.join();
     return plan;
 }
 

@@ -82,6 +82,12 @@ int ibxo_kernel_from_name(const char* name);
 /* Fortran NINT (round half away from zero), as the reference's routines use. */
 int ibxo_nint(double a);
 
+/* One dimension of a kernel's stencil as the Fortran routines compute it:
+ * indices base+i for i in [start, stop] (clipped to the ghost box
+ * [ilower-ghost, iupper+ghost]), w[i] their weights. */
+int ibxo_stencil_1d(int kernel, double X, double Xshift, double x_lower, double dx, int ilower, int iupper, int ghost,
+                    int* base, int* start, int* stop, double* w);
+
 /* Literal restatement of lagrangian_<kernel>_interp{2,3}d / _spread{2,3}d.
  * Arguments carry the Fortran meaning (LEI:481-599); arrays are plain
  * pointers, scalars by value.  ilower/iupper/nugc have dim entries. */

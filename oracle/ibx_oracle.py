@@ -59,6 +59,8 @@ def lib():
         L.ibxo_min_ghost_width.argtypes = [ctypes.c_int]
         L.ibxo_kernel_from_name.argtypes = [ctypes.c_char_p]
         L.ibxo_nint.argtypes = [ctypes.c_double]
+        L.ibxo_stencil_1d.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip, _ip, _dp]
         L.ibxo_fortran_interp.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _ip, _ip, _dp,
                                           _ip, _dp, ctypes.c_int, _dp, _dp]
         L.ibxo_fortran_spread.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp,
@@ -115,6 +117,16 @@ def min_ghost_width(kernel):
 
 def nint(a):
     return lib().ibxo_nint(float(a))
+
+
+def stencil_1d(kernel, X, Xshift, x_lower, dx, ilower, iupper, ghost):
+    """(base, start, stop, weights[6]) of one dimension (Fortran rules)."""
+    b, st, sp = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    w = np.zeros(6)
+    rc = lib().ibxo_stencil_1d(kernel_id(kernel), float(X), float(Xshift), float(x_lower), float(dx), int(ilower),
+                               int(iupper), int(ghost), ctypes.byref(b), ctypes.byref(st), ctypes.byref(sp), dptr(w))
+    assert rc == 0
+    return b.value, st.value, sp.value, w
 
 
 def mt19937_uniform(seed, n, a=0.0, b=1.0):
@@ -244,43 +256,54 @@ def accumulate_ghosts_single_patch(q, domain_lo, domain_hi, periodic):
 # Periodic single-patch problems in the compact layout the CUDA path uses.
 # ---------------------------------------------------------------------------
 
-def periodic_side_problem(dim, N, kernel, X, F=None, u=None):
+def periodic_problem(dim, N, kernel, X, F=None, u=None, centering=1, depth=1):
     """Reference flow on one periodic patch covering [0,1)^dim (LDataManager):
-    spread F of the ghost-box markers (with periodic shifts) into zeroed side
+    spread F of the ghost-box markers (with periodic shifts) into zeroed patch
     data and keep the interior; interpolate u (ghosts filled periodically) at
-    the interior markers.  f/u are compact side arrays, shape (dim,) + N[::-1]
-    (face N == face 0).  Returns (f, U) (None for the parts not requested)."""
+    the interior markers.  f/u are compact periodic arrays of shape
+    (ncomp,) + N[::-1] where ncomp = dim for side data (face N == face 0) and
+    depth for cell data.  Returns (f, U) (None for the parts not requested)."""
     Nl = list(N)
     P = make_patch(dim, [0] * dim, [n - 1 for n in Nl], [0.0] * dim, [1.0] * dim, dx=[1.0 / n for n in Nl],
                    periodic=[1] * dim)
     g = min_ghost_width(kernel)
     gw = [g] * dim
+    Q_depth = dim if centering == 1 else depth
+    q_depth = 1 if centering == 1 else depth
+    ncomp = dim if centering == 1 else depth
     f_out = U_out = None
+
+    def comp_view(q, c):
+        # side: array c, depth 0; cell: array 0, depth c
+        return q.arrays[c][0] if centering == 1 else q.arrays[0][c]
+
     if F is not None:
         idx, sh = cache_local_indices(P, Nl, gw, 1, X)
-        q = GhostedData(P, 1, gw)
-        rc = spread_idx(q, F, dim, X, idx, sh, kernel)
+        q = GhostedData(P, centering, gw, depth=q_depth)
+        rc = spread_idx(q, F, Q_depth, X, idx, sh, kernel)
         assert rc == 0, rc
-        f_out = np.empty([dim] + Nl[::-1])
-        for a in range(dim):
-            sl = tuple([0] + [slice(g, g + n) for n in Nl[::-1]])
-            f_out[a] = q.arrays[a][sl]
+        f_out = np.empty([ncomp] + Nl[::-1])
+        sl = tuple(slice(g, g + n) for n in Nl[::-1])
+        for c in range(ncomp):
+            f_out[c] = comp_view(q, c)[sl]
     if u is not None:
-        q = GhostedData(P, 1, gw)
-        for a in range(dim):
-            arr = q.arrays[a][0]
-            # every ghosted position gets the value of its periodic image
+        q = GhostedData(P, centering, gw, depth=q_depth)
+        for c in range(ncomp):
+            arr = comp_view(q, c)
             grids = np.meshgrid(*[np.arange(arr.shape[k]) for k in range(dim)], indexing="ij")
             src = []
             for k in range(dim):  # numpy axis k <-> dim (dim-1-k)
-                d = dim - 1 - k
-                src.append((grids[k] - g) % Nl[d])
-            arr[...] = u[a][tuple(src)]
+                src.append((grids[k] - g) % Nl[dim - 1 - k])
+            arr[...] = u[c][tuple(src)]
         idx, sh = cache_local_indices(P, Nl, gw, 0, X)
-        U_out = np.zeros(X.size)
-        rc = interpolate_idx(U_out, dim, X, idx, sh, q, kernel)
+        U_out = np.zeros((X.size // dim) * Q_depth)
+        rc = interpolate_idx(U_out, Q_depth, X, idx, sh, q, kernel)
         assert rc == 0, rc
     return f_out, U_out
+
+
+def periodic_side_problem(dim, N, kernel, X, F=None, u=None):
+    return periodic_problem(dim, N, kernel, X, F=F, u=u, centering=1)
 
 
 class CpuPlan:

@@ -1,0 +1,206 @@
+"""Binned plan pipeline (mixed precision) against the FP64 oracle.
+
+Bars: stencil bases and the counting sort bit-exact; spread and
+interpolation within 1e-5 relative (max-norm over the grid and over the
+markers) of the FP64 oracle, the tolerance the mixed form is held to.
+"""
+
+import numpy as np
+import pytest
+
+from tests import cases
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+KERNEL_NAMES = ["PIECEWISE_LINEAR", "PIECEWISE_CUBIC", "IB_3", "IB_4", "IB_6", "BSPLINE_4"]
+MIXED_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ibx():
+    from ibamr_gb300 import ibx as m
+
+    assert torch.cuda.is_available()
+    m.lib()
+    return m
+
+
+def seam_markers(rng, n, dim):
+    X = rng.uniform(0.0, 1.0, size=(n, dim))
+    k = n // 8
+    X[:k] = rng.uniform(0.0, 0.03, size=(k, dim))
+    X[k: 2 * k] = rng.uniform(0.97, 1.0, size=(k, dim))
+    return X.reshape(-1)
+
+
+def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth):
+    ncomp = dim if centering == ibx.SIDE else depth
+    shape = list(N)[::-1]
+    dx = [1.0 / v for v in N]
+    X_t = torch.tensor(X, device="cuda")
+    if centering == ibx.SIDE:
+        f_t = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(dim)]
+        u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+        fq, uq = f_t, u_t
+    else:
+        f_t = torch.zeros([depth] + shape, dtype=torch.float32, device="cuda")
+        u_t = torch.tensor(u, dtype=torch.float32, device="cuda")
+        fq, uq = f_t, u_t
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(X.size // dim * ncomp, dtype=torch.float32, device="cuda")
+    mk = lambda q, Q: ibx.make_problem(dim, centering, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N], dx,
+                                       [0.0] * dim, [1.0] * dim, q, X_t, Q, q_depth=1 if centering else depth,
+                                       Q_depth=ncomp)
+    ps = ibx.Plan(mk(fq, F_t), kernel, ibx.MIXED)
+    pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED)
+    ps.bin()
+    ps.spread()
+    pi.bin()
+    pi.interpolate()
+    torch.cuda.synchronize()
+    f = np.stack([t.double().cpu().numpy() for t in f_t]) if centering == ibx.SIDE else f_t.double().cpu().numpy()
+    return f, U_t.double().cpu().numpy(), ps, pi
+
+
+@pytest.mark.parametrize("kernel", KERNEL_NAMES)
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("centering,depth", [(1, 1), (0, 1), (0, 3)])
+def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, depth):
+    rng = np.random.default_rng(11 + dim + 100 * centering + 10 * depth + 1000 * KERNEL_NAMES.index(kernel))
+    N = [32, 24, 20][:dim] if dim == 3 else [48, 40]
+    n = 3000
+    X = seam_markers(rng, n, dim)
+    ncomp = dim if centering == 1 else depth
+    F = rng.standard_normal(n * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth)
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(U, U_ref) <= MIXED_TOL
+    assert ps.status() == ibx.OK and pi.status() == ibx.OK
+    ps.close()
+    pi.close()
+
+
+def expected_bases(oracle, kernel, X, dim, N):
+    """Stencil bases by the oracle's Fortran rules, relative to ilower = 0,
+    both shifted by the multiple of N that puts the cell-centred one in [0, N)."""
+    n = X.size // dim
+    bc = np.zeros((n, 3), dtype=np.int64)
+    bs = np.zeros((n, 3), dtype=np.int64)
+    for s in range(n):
+        for d in range(dim):
+            dx = 1.0 / N[d]
+            b0 = oracle.stencil_1d(kernel, X[dim * s + d], 0.0, 0.0, dx, 0, N[d] - 1, 10 ** 6)[0]
+            b1 = oracle.stencil_1d(kernel, X[dim * s + d], 0.0, 0.0 - 0.5 * dx, dx, 0, N[d] - 1, 10 ** 6)[0]
+            sh = (b0 // N[d]) * N[d]
+            bc[s, d] = b0 - sh
+            bs[s, d] = b1 - sh
+    return bc, bs
+
+
+def adversarial_positions(rng, dim, N, n):
+    """Positions on and one ulp either side of the decision boundaries of the
+    index rules (cell faces, quarter points, cell centres), plus 0, 1-ulp and
+    tiny values, drawn independently per dimension."""
+    cols = []
+    for d in range(dim):
+        base = []
+        for k in range(0, N[d], max(1, N[d] // 16)):
+            for frac in (0.0, 0.25, 0.5, 0.75):
+                x = (k + frac) / N[d]
+                base += [x, np.nextafter(x, -1.0), np.nextafter(x, 2.0)]
+        base += [0.0, np.nextafter(1.0, 0.0), 5e-324, 1e-300]
+        base = np.array([b for b in base if 0.0 <= b < 1.0])
+        cols.append(rng.choice(base, size=n))
+    return np.stack(cols, axis=1).reshape(-1)
+
+
+@pytest.mark.parametrize("kernel", KERNEL_NAMES)
+@pytest.mark.parametrize("dim", [2, 3])
+def test_binning_bit_exact(ibx, oracle, kernel, dim):
+    rng = np.random.default_rng(5 + dim + 17 * KERNEL_NAMES.index(kernel))
+    N = [64, 64, 64][:dim] if dim == 3 else [128, 96]
+    n = 4000
+    X = np.concatenate([rng.uniform(0.0, 1.0, size=n * dim), adversarial_positions(rng, dim, N, n)])
+    n = X.size // dim
+    F = np.zeros(n * dim)
+    u = np.zeros([dim] + list(N)[::-1])
+    _, _, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, 1, 1)
+    bc, bs, ht, ts, hl = ps.bins(n)
+    ebc, ebs = expected_bases(oracle, kernel, X, dim, N)
+    assert np.array_equal(bc.reshape(n, 3)[:, :dim], ebc[:, :dim])
+    assert np.array_equal(bs.reshape(n, 3)[:, :dim], ebs[:, :dim])
+    # counting sort: tile_start is the exclusive scan of the home-tile counts,
+    # and every tile's segment holds exactly its markers.
+    counts = np.bincount(ht, minlength=ps.n_tiles)
+    assert ts[0] == 0 and np.array_equal(np.diff(ts), counts)
+    assert np.array_equal(np.sort(hl), np.arange(n))
+    for t in rng.choice(ps.n_tiles, size=min(64, ps.n_tiles), replace=False):
+        seg = hl[ts[t]:ts[t + 1]]
+        assert np.all(ht[seg] == t)
+    ps.close()
+    pi.close()
+
+
+def test_batched_plan_matches_per_problem(ibx, oracle):
+    """Several problems of different sizes in one plan give the oracle's
+    answer for each (the batched form used for many independent problems)."""
+    rng = np.random.default_rng(99)
+    dim, kernel = 2, "IB_4"
+    sizes = [32, 64, 48, 128]
+    X_t, F_t, U_t, f_t, u_t, probs_s, probs_i, refs = [], [], [], [], [], [], [], []
+    for N0 in sizes:
+        N = [N0, N0]
+        n = int(rng.integers(100, 2000))
+        X = seam_markers(rng, n, dim)
+        F = rng.standard_normal(n * dim)
+        u = rng.standard_normal([dim, N0, N0])
+        refs.append(oracle.periodic_problem(dim, N, kernel, X, F=F, u=u))
+        xt = torch.tensor(X, device="cuda")
+        ft = [torch.zeros([N0, N0], dtype=torch.float32, device="cuda") for _ in range(dim)]
+        ut = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+        Ft = torch.tensor(F, dtype=torch.float32, device="cuda")
+        Ut = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+        dx = [1.0 / N0] * 2
+        probs_s.append(ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [N0 - 1] * 2, dx, [0, 0], [1, 1], ft,
+                                        xt, Ft))
+        probs_i.append(ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [N0 - 1] * 2, dx, [0, 0], [1, 1], ut,
+                                        xt, Ut))
+        f_t.append(ft)
+        U_t.append(Ut)
+    ps = ibx.Plan(probs_s, kernel, ibx.MIXED)
+    pi = ibx.Plan(probs_i, kernel, ibx.MIXED)
+    ps.bin()
+    ps.spread()
+    pi.bin()
+    pi.interpolate()
+    torch.cuda.synchronize()
+    for k in range(len(sizes)):
+        f = np.stack([t.double().cpu().numpy() for t in f_t[k]])
+        assert cases.rel_err(f, refs[k][0]) <= MIXED_TOL
+        assert cases.rel_err(U_t[k].double().cpu().numpy(), refs[k][1]) <= MIXED_TOL
+    ps.close()
+    pi.close()
+
+
+def test_nonfinite_marker_is_reported_and_skipped(ibx, oracle):
+    rng = np.random.default_rng(3)
+    dim, N, kernel = 3, [16, 16, 16], "IB_4"
+    n = 500
+    X = rng.uniform(0, 1, size=n * dim)
+    X[7 * dim + 1] = np.nan
+    F = rng.standard_normal(n * dim)
+    F[7 * dim: 8 * dim] = 0.0
+    u = rng.standard_normal([dim] + N)
+    keep = np.ones(n, bool)
+    keep[7] = False
+    Xk = X.reshape(n, dim)[keep].reshape(-1)
+    f_ref, _ = oracle.periodic_problem(dim, N, kernel, Xk, F=F.reshape(n, dim)[keep].reshape(-1), u=u)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, 1, 1)
+    assert ps.status() == ibx.E_NONFINITE
+    assert ps.status() == ibx.OK  # the word is cleared by reading it
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    ps.close()
+    pi.close()
