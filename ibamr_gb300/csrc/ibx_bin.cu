@@ -192,6 +192,29 @@ visit_tile_id(const PlanProb& P, int (*tl)[4], const int* nt, int k)
     return P.tile0 + tl[0][c0] + P.ntile[0] * (tl[1][c1] + P.ntile[1] * tl[2][c2]);
 }
 
+// The stencil bases of a record packed into one 64-bit key: markers with
+// equal keys share the stencil of every component.
+template <int DIM>
+__device__ __forceinline__ unsigned long long
+base_key(const Rec& R)
+{
+    unsigned long long k = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+    {
+        k |= (unsigned long long)(unsigned short)R.bc[d] << (16 * d);
+        k |= (unsigned long long)((R.bs[d] - R.bc[d]) & 1) << (48 + d);
+    }
+    return k;
+}
+
+// Lanes of the active set that share both the tile and the stencil key.
+__device__ __forceinline__ unsigned
+unit_group(unsigned act, int tile, unsigned long long key)
+{
+    return __match_any_sync(act, tile) & __match_any_sync(act, key);
+}
+
 template <int DIM, int K>
 __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
 {
@@ -248,19 +271,59 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
         }
     }
     int ht = 0, tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    unsigned long long key = 0;
     if (valid)
     {
         D.rec[g] = R;
         ht = P.tile0 + home[0] + P.ntile[0] * (home[1] + (DIM == 3 ? P.ntile[1] * home[2] : 0));
         D.home_tile[g] = ht;
         nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+        key = base_key<DIM>(R);
     }
-    agg_add(D.hcount, ht, valid);
-    for (int k = 0; __any_sync(0xffffffff, k < nvis); ++k)
+    {
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        bool lead = false;
+        if (valid)
+        {
+            const unsigned grp = unit_group(act, ht, key);
+            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
+        }
+        agg_add(D.hcount, ht, valid);
+        agg_add(D.hucount, ht, lead);
+    }
+    for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
-        agg_add(D.vcount, v ? visit_tile_id<DIM>(P, tl, nt, k) : 0, v);
+        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
+        const unsigned act = __ballot_sync(0xffffffffu, v);
+        bool lead = false;
+        if (v)
+        {
+            const unsigned grp = unit_group(act, t, key);
+            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
+        }
+        agg_add(D.vcount, t, v);
+        agg_add(D.ucount, t, lead);
     }
+}
+
+// Places a unit group: its leader reserves a contiguous range of the list
+// and one unit record; returns the lane's slot in the list.
+__device__ __forceinline__ int
+place_group(unsigned grp, int tile, int* cursor, const int* start, int* ucursor, const int* ustart, int2* units)
+{
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (lane == leader)
+    {
+        const int n = __popc(grp);
+        base = start[tile] + atomicAdd(&cursor[tile], n);
+        const int u = ustart[tile] + atomicAdd(&ucursor[tile], 1);
+        units[u] = make_int2(base, n);
+    }
+    base = __shfl_sync(grp, base, leader);
+    return base + __popc(grp & ((1u << lane) - 1));
 }
 
 template <int DIM, int K>
@@ -273,21 +336,31 @@ __global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
     const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
     const PlanProb& P = D.probs[p];
     int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    unsigned long long key = 0;
     if (valid)
     {
         const Rec R = D.rec[g];
         nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+        key = base_key<DIM>(R);
     }
-    const int hp = agg_add(D.hcursor, valid ? ht : 0, valid);
-    if (valid) D.home_list[D.hcount[ht] + hp] = (int)g;
-    for (int k = 0; __any_sync(0xffffffff, k < nvis); ++k)
+    {
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (valid)
+        {
+            const unsigned grp = unit_group(act, ht, key);
+            const int pos = place_group(grp, ht, D.hcursor, D.hcount, D.hucursor, D.hucount, D.home_units);
+            D.home_list[pos] = (int)g;
+        }
+    }
+    for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
         const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
-        const int r = agg_add(D.vcursor, t, v);
+        const unsigned act = __ballot_sync(0xffffffffu, v);
         if (v)
         {
-            const long long pos = (long long)D.vcount[t] + r;
+            const unsigned grp = unit_group(act, t, key);
+            const int pos = place_group(grp, t, D.vcursor, D.vcount, D.ucursor, D.ucount, D.units);
             if (pos < D.n_visit_cap)
                 D.visit_list[pos] = (int)g;
             else
@@ -295,6 +368,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
         }
     }
 }
+
 // ---- exclusive scan (two levels, exact integer) ---------------------------
 constexpr int SCAN_BLOCK = 1024;
 constexpr int SCAN_ITEMS = 2048; // elements per block
@@ -347,13 +421,15 @@ __global__ void scan_add(int* data, int n, const int* block_offsets)
     if (i < n) data[i] += block_offsets[i / SCAN_ITEMS];
 }
 
-// Spread work items: a tile with c visits gets ceil(c / item_visits) items.
+// Spread work items of the dense-tile kernel: a tile with more than
+// SPARSE_MAX_VISITS visits and u units gets ceil(u / item_units) items.
 __global__ void items_count(const DevPlan D)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= D.n_tiles) return;
     const int c = D.vcount[t + 1] - D.vcount[t];
-    D.items[t] = (c + D.item_visits - 1) / D.item_visits;
+    const int u = D.ucount[t + 1] - D.ucount[t];
+    D.items[t] = c > SPARSE_MAX_VISITS ? (u + D.item_units - 1) / D.item_units : 0;
 }
 
 __global__ void items_fill(const DevPlan D)
@@ -361,6 +437,22 @@ __global__ void items_fill(const DevPlan D)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= D.n_tiles) return;
     for (int k = D.items[t]; k < D.items[t + 1] && k < D.n_item_cap; ++k) D.item_tile[k] = t;
+}
+
+// Interpolation work items: a home tile with u units gets ceil(u / item_units).
+__global__ void hitems_count(const DevPlan D)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= D.n_tiles) return;
+    const int u = D.hucount[t + 1] - D.hucount[t];
+    D.hitems[t] = (u + D.item_units - 1) / D.item_units;
+}
+
+__global__ void hitems_fill(const DevPlan D)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= D.n_tiles) return;
+    for (int k = D.hitems[t]; k < D.hitems[t + 1] && k < D.n_hitem_cap; ++k) D.hitem_tile[k] = t;
 }
 } // namespace
 
@@ -393,6 +485,17 @@ int
 launch_items_fill(const DevPlan& D, cudaStream_t s)
 {
     items_fill<<<(D.n_tiles + 255) / 256, 256, 0, s>>>(D);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+int
+launch_hitems(const DevPlan& D, cudaStream_t s, bool fill)
+{
+    const int blocks = (D.n_tiles + 255) / 256;
+    if (fill)
+        hitems_fill<<<blocks, 256, 0, s>>>(D);
+    else
+        hitems_count<<<blocks, 256, 0, s>>>(D);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 

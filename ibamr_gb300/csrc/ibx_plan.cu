@@ -28,16 +28,7 @@ int build_prob(const ibx_problem& in, int kernel, bool spread, Prob& P);
 
 namespace
 {
-constexpr int ITEM_VISITS = 2048; // default visits per spread work item
-
-int
-item_visits_setting()
-{
-    // IBX_ITEM_VISITS overrides the default (tuning knob; >= 256).
-    const char* e = std::getenv("IBX_ITEM_VISITS");
-    const int v = e ? std::atoi(e) : 0;
-    return v >= 256 ? v : ITEM_VISITS;
-}
+constexpr int ITEM_UNITS = 256; // units per dense spread work item (one per thread)
 
 int
 ceil_log2(long double v)
@@ -188,8 +179,8 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
         visit_cap += (long long)in.n_markers * per;
     }
     if (moffs[n_problems] > 0x7fffffffLL) return IBX_E_TOO_LARGE;
-    const int item_visits = item_visits_setting();
-    const long long item_cap = toffs[n_problems] + visit_cap / item_visits + 1;
+    const long long item_cap = toffs[n_problems] + visit_cap / ITEM_UNITS + 1;
+    const long long hitem_cap = toffs[n_problems] + moffs[n_problems] / ITEM_UNITS + 1;
     if (item_cap > 0x7fffffffLL || visit_cap > 0x7fffffffLL) return IBX_E_TOO_LARGE;
     ibx_plan* plan = new (std::nothrow) ibx_plan;
     if (!plan) return IBX_E_OOM;
@@ -213,11 +204,13 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     const size_t o_toffs = take(sizeof(int) * (n_problems + 1));
     const size_t o_rec = take(sizeof(Rec) * nm);
     const size_t o_home_tile = take(sizeof(int) * nm);
-    // hcount, vcount (+1 each), both cursors, items (+1): zeroed together every step
-    const size_t o_counts = take(sizeof(int) * (5 * (size_t)nt + 3));
+    const size_t o_counts = take(sizeof(int) * counter_ints(nt));
     const size_t o_item_tile = take(sizeof(int) * item_cap);
+    const size_t o_hitem_tile = take(sizeof(int) * hitem_cap);
     const size_t o_home_list = take(sizeof(int) * nm);
     const size_t o_visit = take(sizeof(int) * visit_cap);
+    const size_t o_home_units = take(sizeof(int2) * nm);
+    const size_t o_units = take(sizeof(int2) * visit_cap);
     const size_t o_status = take(sizeof(int) * 4);
     const size_t o_scan = take(sizeof(int) * 2048);
     void* dmem = nullptr;
@@ -249,12 +242,21 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     int* counts = reinterpret_cast<int*>(b + o_counts);
     D.hcount = counts;
     D.vcount = counts + (nt + 1);
-    D.hcursor = counts + 2 * (nt + 1);
-    D.vcursor = counts + 2 * (nt + 1) + nt;
-    D.items = counts + 2 * (nt + 1) + 2 * nt;
+    D.hucount = counts + 2 * (nt + 1);
+    D.ucount = counts + 3 * (nt + 1);
+    D.hcursor = counts + 4 * (nt + 1);
+    D.vcursor = D.hcursor + nt;
+    D.hucursor = D.vcursor + nt;
+    D.ucursor = D.hucursor + nt;
+    D.items = D.ucursor + nt;
+    D.hitems = D.items + (nt + 1);
+    D.hitem_tile = reinterpret_cast<int*>(b + o_hitem_tile);
+    D.n_hitem_cap = (int)hitem_cap;
+    D.home_units = reinterpret_cast<int2*>(b + o_home_units);
+    D.units = reinterpret_cast<int2*>(b + o_units);
     D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
     D.n_item_cap = (int)item_cap;
-    D.item_visits = item_visits;
+    D.item_units = ITEM_UNITS;
     D.home_list = reinterpret_cast<int*>(b + o_home_list);
     D.visit_list = reinterpret_cast<int*>(b + o_visit);
     D.n_visit_cap = visit_cap;
@@ -275,14 +277,19 @@ ibx_plan_bin(ibx_plan* plan, void* stream)
     DevPlan& D = plan->D;
     const int nt = D.n_tiles;
     // Counters, cursors and item counts are contiguous: one memset.
-    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * (5 * (size_t)nt + 3), s) != cudaSuccess) return IBX_E_CUDA;
+    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
     int rc = launch_bin(plan->dim, plan->kernel, D, s, false);
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, plan->scan_tmp, s);
     if (!rc) rc = exclusive_scan(D.vcount, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = exclusive_scan(D.hucount, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = exclusive_scan(D.ucount, nt + 1, plan->scan_tmp, s);
     if (!rc) rc = launch_bin(plan->dim, plan->kernel, D, s, true);
     if (!rc) rc = launch_items(D, s);
     if (!rc) rc = exclusive_scan(D.items, nt + 1, plan->scan_tmp, s);
     if (!rc) rc = launch_items_fill(D, s);
+    if (!rc) rc = launch_hitems(D, s, false);
+    if (!rc) rc = exclusive_scan(D.hitems, nt + 1, plan->scan_tmp, s);
+    if (!rc) rc = launch_hitems(D, s, true);
     return rc;
 }
 

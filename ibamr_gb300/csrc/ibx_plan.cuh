@@ -8,6 +8,9 @@ namespace ibx
 {
 constexpr int TILE3 = 8;  // tile edge in 3D (cells)
 constexpr int TILE2 = 16; // tile edge in 2D
+// Tiles with at most this many visits are spread by the warp-per-tile
+// kernel, larger ones by the unit kernel (one CTA per work item).
+constexpr int SPARSE_MAX_VISITS = 96;
 
 template <int DIM>
 struct TileT
@@ -72,19 +75,39 @@ struct DevPlan
     int n_tiles;
     Rec* rec;         // [n_markers], original marker order
     int* home_tile;   // [n_markers]
-    int* hcount;      // [n_tiles+1], scanned in place into start offsets
-    int* vcount;      // [n_tiles+1]
+    // Counters (zeroed together each step; the *count arrays are scanned in
+    // place into start offsets).
+    int* hcount;      // [n_tiles+1] markers per home tile
+    int* vcount;      // [n_tiles+1] visits per tile
+    int* hucount;     // [n_tiles+1] home units per tile
+    int* ucount;      // [n_tiles+1] visit units per tile
     int* hcursor;     // [n_tiles]
     int* vcursor;     // [n_tiles]
+    int* hucursor;    // [n_tiles]
+    int* ucursor;     // [n_tiles]
+    int* items;       // [n_tiles+1] dense-tile spread work items, scanned into offsets
+    int* hitems;      // [n_tiles+1] interpolation work items per home tile, scanned
     int* home_list;   // [n_markers] global marker ids grouped by home tile
     int* visit_list;  // [n_visit_cap] global marker ids grouped by visited tile
     long long n_visit_cap;
-    int* items;       // [n_tiles+1] spread work items per tile, scanned into offsets
+    // A unit is a run of consecutive list entries that share the tile and
+    // every stencil base: (start in the list, length).
+    int2* home_units; // [n_markers]
+    int2* units;      // [n_visit_cap]
     int* item_tile;   // [n_item_cap] tile of each work item
     int n_item_cap;
-    int item_visits;  // visits per spread work item
+    int* hitem_tile;  // [n_hitem_cap] home tile of each interpolation work item
+    int n_hitem_cap;
+    int item_units;   // units per spread work item (one per thread)
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
+
+// Number of ints of the counter block starting at hcount.
+__host__ __device__ inline size_t
+counter_ints(int n_tiles)
+{
+    return 10 * (size_t)n_tiles + 6;
+}
 
 template <typename T>
 __device__ __forceinline__ int
@@ -190,6 +213,7 @@ int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatt
 int exclusive_scan(int* data, int n, int* tmp, cudaStream_t s);
 int launch_items(const DevPlan& D, cudaStream_t s);
 int launch_items_fill(const DevPlan& D, cudaStream_t s);
+int launch_hitems(const DevPlan& D, cudaStream_t s, bool fill);
 int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
 int launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s);
 

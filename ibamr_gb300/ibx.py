@@ -10,7 +10,7 @@ import ctypes
 import os
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "lib", "libibx.so")
+LIB_PATH = os.environ.get("IBX_LIB_PATH") or os.path.join(PKG, "lib", "libibx.so")
 
 PIECEWISE_LINEAR, PIECEWISE_CUBIC, IB_3, IB_4, IB_6, BSPLINE_4 = range(6)
 KERNELS = {"PIECEWISE_LINEAR": 0, "PIECEWISE_CUBIC": 1, "IB_3": 2, "IB_4": 3, "IB_6": 4, "BSPLINE_4": 5}
