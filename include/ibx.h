@@ -172,6 +172,27 @@ int ibx_plan_n_tiles(const ibx_plan* plan);
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);
 
+/* ---- allocation-free spreading ----------------------------------------- */
+/* No counterpart in the reference (IBAMR's LEInteractor runs on the CPU and
+ * allocates freely); it exists for callers of this library that cannot
+ * allocate device memory: code running while a CUDA graph is captured with a
+ * fixed memory footprint, real-time or error-handling paths, and embeddings
+ * whose memory pool owns the whole device so that cudaMalloc is not
+ * available to libraries.
+ *
+ * ibx_spread_noalloc: the binned mixed-precision spread of ibx_plan_bin +
+ * ibx_plan_spread for one IBX_MODE_PERIODIC problem (float q and Q), with
+ * every scratch buffer placed in a fixed 6 MiB array inside the library
+ * (held on every GPU that loads it until the process exits).  It calls no
+ * allocating routine.  Limits: at most IBX_NOALLOC_MAX_MARKERS markers and
+ * IBX_NOALLOC_MAX_TILES grid tiles (8^3 cells in 3D, 16^2 in 2D); larger
+ * problems return IBX_E_TOO_LARGE.  The first call on a device looks up the
+ * array's address (make it before any stream capture).  All calls share the
+ * array: calls whose work overlaps on the GPU race and must be serialised. */
+#define IBX_NOALLOC_MAX_MARKERS 32768
+#define IBX_NOALLOC_MAX_TILES 4096
+int ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
