@@ -7,12 +7,24 @@
 #include "ibx_internal.h"
 #include "../../include/ibx.h"
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 namespace ibx
 {
+namespace
+{
+std::atomic<long long> g_launches{ 0 };
+} // namespace
+
+void
+note_launches(int n)
+{
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+
 namespace
 {
 bool
@@ -258,6 +270,43 @@ ibx_status_string(int status)
     default:
         return "unknown status";
     }
+}
+
+int
+ibx_device_alloc(void** ptr, long long bytes)
+{
+    if (!ptr || bytes < 0) return IBX_E_ARG;
+    *ptr = nullptr;
+    if (bytes == 0) return IBX_OK;
+    return cudaMalloc(ptr, (size_t)bytes) == cudaSuccess ? IBX_OK : IBX_E_OOM;
+}
+
+int
+ibx_device_free(void* ptr)
+{
+    return cudaFree(ptr) == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+int
+ibx_memcpy(void* dst, const void* src, long long bytes, int to_device)
+{
+    if (bytes <= 0) return IBX_OK;
+    return cudaMemcpy(dst, src, (size_t)bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost) ==
+                   cudaSuccess
+               ? IBX_OK
+               : IBX_E_CUDA;
+}
+
+long long
+ibx_kernel_launches(void)
+{
+    return ibx::g_launches.load(std::memory_order_relaxed);
+}
+
+int
+ibx_synchronize(void)
+{
+    return cudaDeviceSynchronize() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 int

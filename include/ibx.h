@@ -131,6 +131,20 @@ int ibx_interpolate(const ibx_problem* problems, int n_problems, int kernel, int
  * scratch memory; n_problems > 1 as for ibx_interpolate. */
 int ibx_spread(const ibx_problem* problems, int n_problems, int kernel, int precision, void* stream);
 
+/* ---- host helpers (used by the C++ LEInteractor layer) ----------------- */
+/* Device memory and copies for callers without the CUDA runtime headers:
+ * cudaMalloc / cudaFree / blocking cudaMemcpy (to_device != 0: host to
+ * device) / cudaDeviceSynchronize. */
+int ibx_device_alloc(void** ptr, long long bytes);
+int ibx_device_free(void* ptr);
+int ibx_memcpy(void* dst, const void* src, long long bytes, int to_device);
+int ibx_synchronize(void);
+
+/* Diagnostic without a reference counterpart: number of CUDA kernels this
+ * library has launched in the process so far (host-side count, all threads,
+ * all devices). */
+long long ibx_kernel_launches(void);
+
 /* ---- binned plans (the fast path) ------------------------------------- */
 /* A plan owns the scratch memory of the binned spread/interpolate pipeline
  * for a fixed set of IBX_MODE_PERIODIC problems (grids, marker arrays and

@@ -1,0 +1,85 @@
+"""CPU checks of the C-ABI boundary: libibx.so loads, exports every function
+that include/*.h declares, the host-only queries answer like the reference's
+LEInteractor (ibtk/src/lagrangian/LEInteractor.cpp:184-235), and the C++
+LEInteractor layer (include/ibx_leinteractor.h) compiles in 2D and 3D."""
+
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+
+@pytest.fixture(scope="session")
+def libibx():
+    from ibamr_gb300 import build
+
+    if not os.path.exists(build.LIB):
+        build.build()
+    return build.LIB
+
+
+def declared_functions():
+    names = set()
+    for f in os.listdir(INCLUDE):
+        if not f.endswith(".h") or f == "ibx_leinteractor.h":
+            continue
+        text = open(os.path.join(INCLUDE, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        names.update(re.findall(r"\b(ibx_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(libibx):
+    names = declared_functions()
+    assert "ibx_spread" in names and "ibx_plan_create2" in names and "ibx_spread_noalloc" in names
+    out = subprocess.run(["nm", "-D", "--defined-only", libibx], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    L = ctypes.CDLL(libibx)
+    for n in names:
+        getattr(L, n)
+
+
+def test_host_queries(libibx):
+    L = ctypes.CDLL(libibx)
+    L.ibx_status_string.restype = ctypes.c_char_p
+    # LEInteractor::getStencilSize / getMinimumGhostWidth
+    expect = {b"PIECEWISE_LINEAR": (2, 2), b"PIECEWISE_CUBIC": (4, 3), b"IB_3": (4, 3),
+              b"IB_4": (4, 3), b"IB_6": (6, 4), b"BSPLINE_4": (4, 3)}
+    for name, (width, ghost) in expect.items():
+        k = L.ibx_kernel_from_name(name)
+        assert k >= 0
+        assert L.ibx_get_stencil_size(k) == width
+        assert L.ibx_get_minimum_ghost_width(k) == ghost
+    assert L.ibx_kernel_from_name(b"IB_5") == -1
+    assert L.ibx_get_stencil_size(99) == -1
+    assert L.ibx_status_string(0) == b"success"
+    assert L.ibx_status_string(1) == b"unknown kernel function"
+
+
+CPP_TEST = os.path.join(ROOT, "tests", "cpp", "leinteractor_test.cpp")
+
+
+def compile_cpp_test(libibx, dim, out):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    libdir = os.path.dirname(libibx)
+    cmd = [gxx, "-std=c++17", "-O2", "-Wall", "-DNDIM=%d" % dim, "-I", INCLUDE, CPP_TEST,
+           "-L", libdir, "-libx", "-Wl,-rpath," + libdir, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cpp_leinteractor_layer_compiles(libibx, tmp_path, dim):
+    compile_cpp_test(libibx, dim, str(tmp_path / ("lei%d" % dim)))
