@@ -233,11 +233,13 @@ def run_ours(args):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = ibx.kernel_launches()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
+    launches = ibx.kernel_launches() - launches0
     barrier()
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
@@ -246,7 +248,6 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * n / (ms * 1e-3)
-    launches_per_step = 3 + 3 + 2 + 1 + 1  # bin, scan x2 (<=3 each), scatter, spread, interp
 
     # ---- per-phase timing (same stream) for the roofline --------------------
     def timed(fn, reps):
@@ -352,7 +353,7 @@ def run_ours(args):
             "plain_fp64": {"value": n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -468,6 +468,7 @@ exclusive_scan(int* data, int n, int* tmp, cudaStream_t s)
         scan_blocks<<<1, SCAN_BLOCK, 0, s>>>(tmp, nb, nullptr);
         scan_add<<<(n + 255) / 256, 256, 0, s>>>(data, n, tmp);
     }
+    note_launches(nb > 1 ? 3 : 1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
@@ -476,6 +477,7 @@ launch_items(const DevPlan& D, cudaStream_t s)
 {
     const int blocks = (D.n_tiles + 255) / 256;
     items_count<<<blocks, 256, 0, s>>>(D);
+    note_launches(1);
     if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
     // items[n_tiles] was zeroed with the counters; the scan turns counts into offsets.
     return IBX_OK;
@@ -485,6 +487,7 @@ int
 launch_items_fill(const DevPlan& D, cudaStream_t s)
 {
     items_fill<<<(D.n_tiles + 255) / 256, 256, 0, s>>>(D);
+    note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
@@ -496,6 +499,7 @@ launch_hitems(const DevPlan& D, cudaStream_t s, bool fill)
         hitems_fill<<<blocks, 256, 0, s>>>(D);
     else
         hitems_count<<<blocks, 256, 0, s>>>(D);
+    note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
@@ -511,6 +515,7 @@ launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter)
             scatter_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                        \
         else                                                                                                         \
             bin_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                            \
+        note_launches(1);                                                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
     }
     IBX_BIN_CASE(2, K_PL) IBX_BIN_CASE(2, K_PCUBIC) IBX_BIN_CASE(2, K_IB3) IBX_BIN_CASE(2, K_IB4)

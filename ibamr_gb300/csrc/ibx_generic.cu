@@ -157,6 +157,7 @@ launch_dk(bool spread, const ProbArg& A, cudaStream_t stream)
         generic_fp64_kernel<DIM, K, true><<<(unsigned)blocks, threads, 0, stream>>>(A);
     else
         generic_fp64_kernel<DIM, K, false><<<(unsigned)blocks, threads, 0, stream>>>(A);
+    note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 

@@ -18,6 +18,9 @@ struct ProbArg
     long long total;
 };
 
+// Host-side count of the kernels libibx has launched (ibx_kernel_launches()).
+void note_launches(int n);
+
 // Generic (marker-parallel, reference-faithful FP64) spread / interpolate.
 int launch_generic(bool spread, int dim, int kernel, const ProbArg& arg, cudaStream_t stream);
 

@@ -134,6 +134,7 @@ launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s)
     if (dim == DD && kernel == KK)                                                                                   \
     {                                                                                                                \
         interp_home_mixed<DD, KK><<<grid, INTERP_THREADS, 0, s>>>(D);                                                \
+        note_launches(1);                                                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
     }
     IBX_INTERP_CASE(2, K_PL) IBX_INTERP_CASE(2, K_PCUBIC) IBX_INTERP_CASE(2, K_IB3) IBX_INTERP_CASE(2, K_IB4)

@@ -386,12 +386,14 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
             spread_units_mixed<DD, KK><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);                                  \
         else                                                                                                         \
             spread_visits_mixed<DD, KK><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);                                 \
+        note_launches(1);                                                                                            \
         if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;                                                   \
         if (smem_sparse > 48 * 1024 &&                                                                               \
             cudaFuncSetAttribute(spread_sparse_mixed<DD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                  (int)smem_sparse) != cudaSuccess)                                                   \
             return IBX_E_CUDA;                                                                                       \
         spread_sparse_mixed<DD, KK><<<sparse_blocks, 32 * SPARSE_WARPS, smem_sparse, s>>>(D);                        \
+        note_launches(1);                                                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
     }
     IBX_SPREAD_CASE(2, K_PL) IBX_SPREAD_CASE(2, K_PCUBIC) IBX_SPREAD_CASE(2, K_IB3) IBX_SPREAD_CASE(2, K_IB4)

@@ -59,6 +59,7 @@ def lib():
         L.ibx_kernel_from_name.argtypes = [ctypes.c_char_p]
         L.ibx_status_string.argtypes = [ctypes.c_int]
         L.ibx_status_string.restype = ctypes.c_char_p
+        L.ibx_kernel_launches.restype = ctypes.c_longlong
         for name in ("ibx_interpolate", "ibx_spread"):
             getattr(L, name).argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         if hasattr(L, "ibx_plan_create"):
@@ -84,6 +85,11 @@ def status_string(status):
         return lib().ibx_status_string(int(status)).decode()
     except Exception:  # library missing
         return "status %d" % status
+
+
+def kernel_launches():
+    """Number of CUDA kernels libibx has launched in this process."""
+    return int(lib().ibx_kernel_launches())
 
 
 def kernel_id(kernel):
