@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=float, default=0.1, help="fraction of markers for the CPU baseline")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     return ap.parse_args()
 
 
@@ -214,6 +215,11 @@ def run_ours(args):
                                 q, Xq, Q)
 
     plan = ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)])
+    tuned = None
+    if not args.no_tune:
+        from ibamr_gb300 import tuning
+
+        tuned = tuning.autotune(plan)
 
     def step():
         plan.bin()
@@ -290,6 +296,7 @@ def run_ours(args):
     # ---- accuracy of the mixed form against the plain FP64 form -------------
     f_t2 = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
     plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED)
+    plan_e.set_tuning(*plan.tuning())
     plan_e.bin()
     plan_e.spread()
     fd = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
@@ -353,6 +360,10 @@ def run_ours(args):
             "plain_fp64": {"value": n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
+            "tuning": None if tuned is None else {
+                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
+                "bin_spread_ms": tuned["ms"],
+                "table": [[list(c), round(t, 4)] for c, t in tuned["table"]]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
         }

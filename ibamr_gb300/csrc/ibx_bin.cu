@@ -215,6 +215,10 @@ unit_group(unsigned act, int tile, unsigned long long key)
     return __match_any_sync(act, tile) & __match_any_sync(act, key);
 }
 
+// Phase 0: one thread per marker derives the record (exact stencil bases
+// and kernel arguments of the cell-centred and staggered positions) and its
+// home tile, and counts the marker and its unit (warp-local run of markers
+// with equal stencil bases) into the home tile.
 template <int DIM, int K>
 __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
 {
@@ -270,41 +274,24 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
             valid = false;
         }
     }
-    int ht = 0, tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    int ht = 0;
     unsigned long long key = 0;
     if (valid)
     {
         D.rec[g] = R;
         ht = P.tile0 + home[0] + P.ntile[0] * (home[1] + (DIM == 3 ? P.ntile[1] * home[2] : 0));
         D.home_tile[g] = ht;
-        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
         key = base_key<DIM>(R);
     }
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    bool lead = false;
+    if (valid)
     {
-        const unsigned act = __ballot_sync(0xffffffffu, valid);
-        bool lead = false;
-        if (valid)
-        {
-            const unsigned grp = unit_group(act, ht, key);
-            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
-        }
-        agg_add(D.hcount, ht, valid);
-        agg_add(D.hucount, ht, lead);
+        const unsigned grp = unit_group(act, ht, key);
+        lead = (threadIdx.x & 31) == __ffs(grp) - 1;
     }
-    for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
-    {
-        const bool v = k < nvis;
-        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
-        const unsigned act = __ballot_sync(0xffffffffu, v);
-        bool lead = false;
-        if (v)
-        {
-            const unsigned grp = unit_group(act, t, key);
-            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
-        }
-        agg_add(D.vcount, t, v);
-        agg_add(D.ucount, t, lead);
-    }
+    agg_add(D.hcount, ht, valid);
+    agg_add(D.hucount, ht, lead);
 }
 
 // Places a unit group: its leader reserves a contiguous range of the list
@@ -326,8 +313,16 @@ place_group(unsigned grp, int tile, int* cursor, const int* start, int* ucursor,
     return base + __popc(grp & ((1u << lane) - 1));
 }
 
+__device__ __forceinline__ bool
+dense_home(const DevPlan& D, int ht)
+{
+    return D.hcount[ht + 1] - D.hcount[ht] > D.dense_min;
+}
+
+// Phase 1: counting sort by home tile (home list, home units and the records
+// in home order); markers of sparse home tiles count their visits.
 template <int DIM, int K>
-__global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
+__global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
 {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     bool valid = g < D.n_markers;
@@ -335,12 +330,12 @@ __global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
     valid = valid && ht >= 0;
     const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
     const PlanProb& P = D.probs[p];
-    int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    Rec R;
     unsigned long long key = 0;
+    int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
     if (valid)
     {
-        const Rec R = D.rec[g];
-        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+        R = D.rec[g];
         key = base_key<DIM>(R);
     }
     {
@@ -350,7 +345,43 @@ __global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
             const unsigned grp = unit_group(act, ht, key);
             const int pos = place_group(grp, ht, D.hcursor, D.hcount, D.hucursor, D.hucount, D.home_units);
             D.home_list[pos] = (int)g;
+            D.hrec[pos] = R;
+            if (!dense_home(D, ht)) nvis = visit_tiles<DIM, K>(P, R, tl, nt);
         }
+    }
+    for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
+    {
+        const bool v = k < nvis;
+        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
+        const unsigned act = __ballot_sync(0xffffffffu, v);
+        bool lead = false;
+        if (v)
+        {
+            const unsigned grp = unit_group(act, t, key);
+            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
+        }
+        agg_add(D.vcount, t, v);
+        agg_add(D.ucount, t, lead);
+    }
+}
+
+// Phase 2: counting sort of the visits of sparse-homed markers by visited tile.
+template <int DIM, int K>
+__global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
+{
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool valid = g < D.n_markers;
+    const int ht = valid ? D.home_tile[g] : -1;
+    valid = valid && ht >= 0 && !dense_home(D, ht);
+    const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
+    const PlanProb& P = D.probs[p];
+    int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
+    unsigned long long key = 0;
+    if (valid)
+    {
+        const Rec R = D.rec[g];
+        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+        key = base_key<DIM>(R);
     }
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
@@ -373,12 +404,13 @@ __global__ void __launch_bounds__(256) scatter_kernel(const DevPlan D)
 constexpr int SCAN_BLOCK = 1024;
 constexpr int SCAN_ITEMS = 2048; // elements per block
 
-__global__ void __launch_bounds__(SCAN_BLOCK) scan_blocks(int* data, int n, int* block_sums)
+// Block-level Blelloch scan of array blockIdx.y (arrays of n ints, stride n).
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_blocks(int* data, int n, int* block_sums, int nb)
 {
     __shared__ int s[SCAN_ITEMS];
+    int* a = data + (long long)blockIdx.y * n;
     const int base = blockIdx.x * SCAN_ITEMS;
-    for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_BLOCK) s[i] = (base + i < n) ? data[base + i] : 0;
-    // Blelloch up-sweep / down-sweep.
+    for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_BLOCK) s[i] = (base + i < n) ? a[base + i] : 0;
     int offset = 1;
     for (int d = SCAN_ITEMS >> 1; d > 0; d >>= 1)
     {
@@ -394,7 +426,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK) scan_blocks(int* data, int n, int*
     __syncthreads();
     if (threadIdx.x == 0)
     {
-        if (block_sums) block_sums[blockIdx.x] = s[SCAN_ITEMS - 1];
+        if (block_sums) block_sums[blockIdx.y * nb + blockIdx.x] = s[SCAN_ITEMS - 1];
         s[SCAN_ITEMS - 1] = 0;
     }
     for (int d = 1; d < SCAN_ITEMS; d <<= 1)
@@ -412,109 +444,76 @@ __global__ void __launch_bounds__(SCAN_BLOCK) scan_blocks(int* data, int n, int*
     }
     __syncthreads();
     for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_BLOCK)
-        if (base + i < n) data[base + i] = s[i];
+        if (base + i < n) a[base + i] = s[i];
 }
 
-__global__ void scan_add(int* data, int n, const int* block_offsets)
+__global__ void scan_add(int* data, int n, const int* block_offsets, int nb)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) data[i] += block_offsets[i / SCAN_ITEMS];
+    if (i < n) data[(long long)blockIdx.y * n + i] += block_offsets[blockIdx.y * nb + i / SCAN_ITEMS];
 }
 
-// Spread work items of the dense-tile kernel: a tile with more than
-// SPARSE_MAX_VISITS visits and u units gets ceil(u / item_units) items.
+// Dense-tile spread work items: a home tile with more than dense_min markers
+// and u home units gets ceil(u / item_units) items.
 __global__ void items_count(const DevPlan D)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= D.n_tiles) return;
-    const int c = D.vcount[t + 1] - D.vcount[t];
-    const int u = D.ucount[t + 1] - D.ucount[t];
-    D.items[t] = c > SPARSE_MAX_VISITS ? (u + D.item_units - 1) / D.item_units : 0;
+    const int u = D.hucount[t + 1] - D.hucount[t];
+    D.items[t] = dense_home(D, t) ? (u + D.item_units - 1) / D.item_units : 0;
 }
 
 __global__ void items_fill(const DevPlan D)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && D.items[D.n_tiles] > D.n_item_cap) atomicOr(D.status, 2);
     if (t >= D.n_tiles) return;
     for (int k = D.items[t]; k < D.items[t + 1] && k < D.n_item_cap; ++k) D.item_tile[k] = t;
 }
-
-// Interpolation work items: a home tile with u units gets ceil(u / item_units).
-__global__ void hitems_count(const DevPlan D)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= D.n_tiles) return;
-    const int u = D.hucount[t + 1] - D.hucount[t];
-    D.hitems[t] = (u + D.item_units - 1) / D.item_units;
-}
-
-__global__ void hitems_fill(const DevPlan D)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= D.n_tiles) return;
-    for (int k = D.hitems[t]; k < D.hitems[t + 1] && k < D.n_hitem_cap; ++k) D.hitem_tile[k] = t;
-}
 } // namespace
 
-// Exclusive scan of data[0..n) in place; tmp holds SCAN_ITEMS ints.
 int
-exclusive_scan(int* data, int n, int* tmp, cudaStream_t s)
+exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s)
 {
     const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
     if (nb > SCAN_ITEMS) return IBX_E_TOO_LARGE; // more than 4M entries
-    scan_blocks<<<nb, SCAN_BLOCK, 0, s>>>(data, n, tmp);
+    scan_blocks<<<dim3(nb, count), SCAN_BLOCK, 0, s>>>(data, n, tmp, nb);
     if (nb > 1)
     {
-        scan_blocks<<<1, SCAN_BLOCK, 0, s>>>(tmp, nb, nullptr);
-        scan_add<<<(n + 255) / 256, 256, 0, s>>>(data, n, tmp);
+        // tmp[a * nb + b]: block sums of array a, scanned per array.
+        scan_blocks<<<dim3(1, count), SCAN_BLOCK, 0, s>>>(tmp, nb, nullptr, 1);
+        scan_add<<<dim3((n + 255) / 256, count), 256, 0, s>>>(data, n, tmp, nb);
     }
     note_launches(nb > 1 ? 3 : 1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 int
-launch_items(const DevPlan& D, cudaStream_t s)
-{
-    const int blocks = (D.n_tiles + 255) / 256;
-    items_count<<<blocks, 256, 0, s>>>(D);
-    note_launches(1);
-    if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
-    // items[n_tiles] was zeroed with the counters; the scan turns counts into offsets.
-    return IBX_OK;
-}
-
-int
-launch_items_fill(const DevPlan& D, cudaStream_t s)
-{
-    items_fill<<<(D.n_tiles + 255) / 256, 256, 0, s>>>(D);
-    note_launches(1);
-    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
-}
-
-int
-launch_hitems(const DevPlan& D, cudaStream_t s, bool fill)
+launch_items(const DevPlan& D, cudaStream_t s, bool fill)
 {
     const int blocks = (D.n_tiles + 255) / 256;
     if (fill)
-        hitems_fill<<<blocks, 256, 0, s>>>(D);
+        items_fill<<<blocks, 256, 0, s>>>(D);
     else
-        hitems_count<<<blocks, 256, 0, s>>>(D);
+        items_count<<<blocks, 256, 0, s>>>(D);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 int
-launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter)
+launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 {
     const unsigned blocks = (unsigned)((D.n_markers + 255) / 256);
     if (blocks == 0) return IBX_OK;
 #define IBX_BIN_CASE(DD, KK)                                                                                         \
     if (dim == DD && kernel == KK)                                                                                   \
     {                                                                                                                \
-        if (scatter)                                                                                                 \
-            scatter_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                        \
-        else                                                                                                         \
+        if (phase == 0)                                                                                              \
             bin_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                            \
+        else if (phase == 1)                                                                                         \
+            scatter_home_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                   \
+        else                                                                                                         \
+            scatter_visits_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                 \
         note_launches(1);                                                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
     }
@@ -523,6 +522,23 @@ launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter)
     IBX_BIN_CASE(3, K_IB3) IBX_BIN_CASE(3, K_IB4) IBX_BIN_CASE(3, K_IB6) IBX_BIN_CASE(3, K_BSPL4)
 #undef IBX_BIN_CASE
     return IBX_E_BAD_KERNEL;
+}
+
+int
+bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s)
+{
+    const int nt = D.n_tiles;
+    // Counters, cursors and item counts are contiguous: one memset.
+    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
+    int rc = launch_bin(dim, kernel, D, s, 0);
+    if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
+    if (!rc) rc = launch_bin(dim, kernel, D, s, 1);
+    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 2, scan_tmp, s); // vcount, ucount
+    if (!rc) rc = launch_bin(dim, kernel, D, s, 2);
+    if (!rc) rc = launch_items(D, s, false);
+    if (!rc) rc = exclusive_scan(D.items, nt + 1, 1, scan_tmp, s);
+    if (!rc) rc = launch_items(D, s, true);
+    return rc;
 }
 
 } // namespace ibx

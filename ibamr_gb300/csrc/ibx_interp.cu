@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_home_mixed(const DevPla
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.marker_offs, D.n_probs, (long long)g);
         const PlanProb& P = D.probs[p];
         if (c >= P.ncomp) continue;
-        const Rec R = D.rec[g];
+        const Rec R = D.hrec[m];
         int b[3] = { 0, 0, 0 };
         float w[3][W];
 #pragma unroll

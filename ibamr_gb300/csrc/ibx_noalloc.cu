@@ -31,8 +31,7 @@ namespace
 // Limits of the allocation-free path.
 constexpr long long NOALLOC_MAX_MARKERS = IBX_NOALLOC_MAX_MARKERS;
 constexpr int NOALLOC_MAX_TILES = IBX_NOALLOC_MAX_TILES;
-constexpr int NOALLOC_UNITS_PER_ITEM = 256;
-constexpr size_t NOALLOC_SCRATCH_BYTES = 6u << 20; // 6 MiB
+constexpr size_t NOALLOC_SCRATCH_BYTES = 8u << 20; // 8 MiB
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
@@ -59,38 +58,6 @@ scratch_address(void** out)
     return IBX_OK;
 }
 
-size_t
-up256(size_t v)
-{
-    return (v + 255) & ~size_t(255);
-}
-
-int
-ceil_log2_ld(long double v)
-{
-    int e = 0;
-    while (std::ldexp(1.0L, e) < v) ++e;
-    return e;
-}
-
-// Constants of the exact fixed-point index path (the rules of ibx_bin.cu).
-bool
-fixed_constants(double x_lower, double x_upper, double dx, ibx::FixedDim& fx)
-{
-    const long double xmax = 2.0L * std::max(std::fabs((long double)x_lower), std::fabs((long double)x_upper)) +
-                             8.0L * dx + 1e-30L;
-    fx.sx = 62 - ceil_log2_ld(xmax);
-    const long double inv = 1.0L / (long double)dx;
-    const int si = 62 - (std::ilogb(inv) + 1);
-    fx.inv_f = std::llround(std::ldexp(inv, si));
-    fx.F = fx.sx + si - 64;
-    const int tb = ceil_log2_ld(xmax * inv + 2.0L);
-    fx.dshift = fx.F - 48 + tb;
-    fx.xlo_c_f = std::llround(std::ldexp((long double)x_lower, fx.sx));
-    const double xlo_s = x_lower - 0.5 * dx;
-    fx.xlo_s_f = std::llround(std::ldexp((long double)xlo_s, fx.sx));
-    return fx.sx > 0 && fx.F >= 24 && fx.F <= 62 && fx.dshift >= 2 && fx.dshift <= fx.F - 4 && tb <= 30;
-}
 } // namespace
 
 namespace ibx
@@ -142,7 +109,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
         P.dx_pow2[d] = chk.dx_pow2[d];
         P.xlo_c[d] = in.x_lower[d];
         P.xlo_s[d] = in.x_lower[d] - 0.5 * in.dx[d];
-        fixed_ok = fixed_constants(in.x_lower[d], in.x_upper[d], in.dx[d], P.fx[d]) && fixed_ok;
+        fixed_ok = fixed_dim(in.x_lower[d], in.x_upper[d], in.dx[d], P.fx[d]) && fixed_ok;
     }
     if (ntiles > NOALLOC_MAX_TILES) return IBX_E_TOO_LARGE;
     P.fixed_ok = fixed_ok ? 1 : 0;
@@ -155,95 +122,41 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
         P.q[c] = P.side ? in.q[c] : static_cast<void*>(static_cast<float*>(in.q[0]) + vol * c);
         P.qi[c] = P.q[c];
     }
+    P.vec4 = P.N[0] % 4 == 0;
+    for (int c = 0; c < ncomp; ++c) P.vec4 = P.vec4 && (reinterpret_cast<unsigned long long>(P.q[c]) & 15) == 0;
     P.tile0 = 0;
     P.marker0 = 0;
 
-    // Carve the scratch array (same buffers as a plan, capacities at the limits).
+    // Carve the scratch array (the buffers of a plan, capacities at the limits).
     const long long nm = in.n_markers;
     const int nt = (int)ntiles;
-    const long long visit_cap = nm * (dim == 3 ? 8 : 4);
-    const long long item_cap = nt + visit_cap / NOALLOC_UNITS_PER_ITEM + 1;
-    const long long hitem_cap = nt + nm / NOALLOC_UNITS_PER_ITEM + 1;
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        const size_t o = off;
-        off = up256(off + bytes);
-        return o;
-    };
-    const size_t o_probs = take(sizeof(PlanProb));
-    const size_t o_moffs = take(sizeof(long long) * 2);
-    const size_t o_toffs = take(sizeof(int) * 2);
-    const size_t o_rec = take(sizeof(Rec) * nm);
-    const size_t o_home_tile = take(sizeof(int) * nm);
-    const size_t o_counts = take(sizeof(int) * counter_ints(nt));
-    const size_t o_item_tile = take(sizeof(int) * item_cap);
-    const size_t o_hitem_tile = take(sizeof(int) * hitem_cap);
-    const size_t o_home_list = take(sizeof(int) * nm);
-    const size_t o_visit = take(sizeof(int) * visit_cap);
-    const size_t o_home_units = take(sizeof(int2) * nm);
-    const size_t o_units = take(sizeof(int2) * visit_cap);
-    const size_t o_status = take(sizeof(int) * 4);
-    const size_t o_scan = take(sizeof(int) * 2048);
-    if (off > NOALLOC_SCRATCH_BYTES) return IBX_E_TOO_LARGE;
+    PlanSizes z;
+    z.n_probs = 1;
+    z.n_markers = nm;
+    z.n_tiles = nt;
+    z.visit_cap = nm * (dim == 3 ? 8 : 4);
+    z.item_cap = nt + nm / 10 + 1;
+    DevPlan D;
+    if (carve_plan(z, nullptr, D).bytes > NOALLOC_SCRATCH_BYTES) return IBX_E_TOO_LARGE;
 
     void* base = nullptr;
     const int rs = scratch_address(&base);
     if (rs) return rs;
     char* b = static_cast<char*>(base);
+    const PlanCarve c = carve_plan(z, b, D);
+    D.item_units = 256 / ncomp;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const long long moffs[2] = { 0, nm };
     const int toffs[2] = { 0, nt };
-    if (cudaMemcpyAsync(b + o_probs, &P, sizeof(P), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b + o_moffs, moffs, sizeof(moffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b + o_toffs, toffs, sizeof(toffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(b + o_status, 0, sizeof(int) * 4, s) != cudaSuccess)
+    // The pageable sources are staged by the runtime before these calls return.
+    if (cudaMemcpyAsync(b + c.o_probs, &P, sizeof(P), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b + c.o_moffs, moffs, sizeof(moffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b + c.o_toffs, toffs, sizeof(toffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(b + c.o_status, 0, sizeof(int) * 4, s) != cudaSuccess)
         return IBX_E_CUDA;
 
-    DevPlan D;
-    std::memset(&D, 0, sizeof(D));
-    D.probs = reinterpret_cast<const PlanProb*>(b + o_probs);
-    D.marker_offs = reinterpret_cast<const long long*>(b + o_moffs);
-    D.tile_offs = reinterpret_cast<const int*>(b + o_toffs);
-    D.n_probs = 1;
-    D.n_markers = nm;
-    D.n_tiles = nt;
-    D.rec = reinterpret_cast<Rec*>(b + o_rec);
-    D.home_tile = reinterpret_cast<int*>(b + o_home_tile);
-    int* counts = reinterpret_cast<int*>(b + o_counts);
-    D.hcount = counts;
-    D.vcount = counts + (nt + 1);
-    D.hucount = counts + 2 * (nt + 1);
-    D.ucount = counts + 3 * (nt + 1);
-    D.hcursor = counts + 4 * (nt + 1);
-    D.vcursor = D.hcursor + nt;
-    D.hucursor = D.vcursor + nt;
-    D.ucursor = D.hucursor + nt;
-    D.items = D.ucursor + nt;
-    D.hitems = D.items + (nt + 1);
-    D.home_list = reinterpret_cast<int*>(b + o_home_list);
-    D.visit_list = reinterpret_cast<int*>(b + o_visit);
-    D.n_visit_cap = visit_cap;
-    D.home_units = reinterpret_cast<int2*>(b + o_home_units);
-    D.units = reinterpret_cast<int2*>(b + o_units);
-    D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
-    D.n_item_cap = (int)item_cap;
-    D.hitem_tile = reinterpret_cast<int*>(b + o_hitem_tile);
-    D.n_hitem_cap = (int)hitem_cap;
-    D.item_units = NOALLOC_UNITS_PER_ITEM;
-    D.status = reinterpret_cast<int*>(b + o_status);
-    int* scan_tmp = reinterpret_cast<int*>(b + o_scan);
-
-    // Counters and cursors start at zero on every call.
-    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
-    int rc = launch_bin(dim, kernel, D, s, false);
-    if (!rc) rc = exclusive_scan(D.hcount, nt + 1, scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.hucount, nt + 1, scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.ucount, nt + 1, scan_tmp, s);
-    if (!rc) rc = launch_bin(dim, kernel, D, s, true);
-    if (!rc) rc = launch_items(D, s);
-    if (!rc) rc = exclusive_scan(D.items, nt + 1, scan_tmp, s);
-    if (!rc) rc = launch_items_fill(D, s);
+    // Counters and cursors are zeroed by the binning sequence on every call.
+    int rc = bin_sequence(dim, kernel, D, c.scan_tmp, s);
     if (!rc) rc = launch_spread(dim, kernel, D, ncomp, s);
     return rc;
 }

@@ -4,12 +4,14 @@
 // Per step:
 //   1. bin (ibx_bin.cu): one thread per marker derives the exact stencil
 //      bases and kernel arguments (cell-centred and staggered position) and
-//      counts the marker into its home tile and into every tile its
-//      footprint touches (warp-aggregated atomics).
-//   2. exclusive scans of both histograms (exact integer).
-//   3. scatter: counting sort into per-tile home lists and visit lists.
-//   4. work items: tiles with many visits are split into several items.
-//   5. spread (ibx_spread.cu): one CTA per work item owns its tile.
+//      counts the marker into its home tile (warp-aggregated atomics).
+//   2. exclusive scans (exact integer).
+//   3. counting sort by home tile; markers of sparse home tiles count the
+//      tiles their footprints touch; scans; counting sort of those visits.
+//   4. work items: dense home tiles are split into items of home units.
+//   5. spread (ibx_spread.cu): dense tiles spread their home markers into a
+//      tile+halo region, sparse-homed markers are spread by the owner of
+//      every tile they visit.
 //   6. interpolate (ibx_interp.cu): markers in home-tile order.
 // Geometry: IBX_MODE_PERIODIC problems (compact periodic arrays).
 
@@ -28,7 +30,11 @@ int build_prob(const ibx_problem& in, int kernel, bool spread, Prob& P);
 
 namespace
 {
-constexpr int ITEM_UNITS = 256; // units per dense spread work item (one per thread)
+constexpr int ITEM_UNITS = 256; // home units per dense spread work item (one per thread)
+constexpr int MIN_ITEM_UNITS = 32; // smallest setting of ibx_plan_set_tuning
+// Items hold ITEM_UNITS / ncomp units by default (one thread per unit and
+// component); the capacity below allows MIN_ITEM_UNITS / 3 per item.
+constexpr int DENSE_MIN = 32;   // home tiles with more markers are spread by home region
 
 int
 ceil_log2(long double v)
@@ -37,6 +43,13 @@ ceil_log2(long double v)
     while (std::ldexp(1.0L, e) < v) ++e;
     return e;
 }
+
+size_t
+align256(size_t v)
+{
+    return (v + 255) & ~size_t(255);
+}
+} // namespace
 
 // Constants of the exact fixed-point index path for one dimension (see
 // ibx_bin.cu); returns false when the problem's range does not fit.
@@ -58,12 +71,69 @@ fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx)
     return fx.sx > 0 && fx.F >= 24 && fx.F <= 62 && fx.dshift >= 2 && fx.dshift <= fx.F - 4 && tb <= 30;
 }
 
-size_t
-align256(size_t v)
+PlanCarve
+carve_plan(const PlanSizes& z, char* b, DevPlan& D)
 {
-    return (v + 255) & ~size_t(255);
+    PlanCarve c;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const long long nm = z.n_markers;
+    const int nt = z.n_tiles;
+    c.o_probs = take(sizeof(PlanProb) * z.n_probs);
+    c.o_moffs = take(sizeof(long long) * (z.n_probs + 1));
+    c.o_toffs = take(sizeof(int) * (z.n_probs + 1));
+    const size_t o_rec = take(sizeof(Rec) * nm);
+    const size_t o_hrec = take(sizeof(Rec) * nm);
+    const size_t o_home_tile = take(sizeof(int) * nm);
+    const size_t o_counts = take(sizeof(int) * counter_ints(nt));
+    const size_t o_item_tile = take(sizeof(int) * z.item_cap);
+    const size_t o_home_list = take(sizeof(int) * nm);
+    const size_t o_visit = take(sizeof(int) * z.visit_cap);
+    const size_t o_home_units = take(sizeof(int2) * nm);
+    const size_t o_units = take(sizeof(int2) * z.visit_cap);
+    c.o_status = take(sizeof(int) * 4);
+    const size_t o_scan = take(sizeof(int) * 4096);
+    c.bytes = off;
+    c.scan_tmp = nullptr;
+    if (!b) return c;
+    std::memset(&D, 0, sizeof(D));
+    D.probs = reinterpret_cast<const PlanProb*>(b + c.o_probs);
+    D.marker_offs = reinterpret_cast<const long long*>(b + c.o_moffs);
+    D.tile_offs = reinterpret_cast<const int*>(b + c.o_toffs);
+    D.n_probs = z.n_probs;
+    D.n_markers = nm;
+    D.n_tiles = nt;
+    D.rec = reinterpret_cast<Rec*>(b + o_rec);
+    D.hrec = reinterpret_cast<Rec*>(b + o_hrec);
+    D.home_tile = reinterpret_cast<int*>(b + o_home_tile);
+    int* counts = reinterpret_cast<int*>(b + o_counts);
+    D.hcount = counts;
+    D.hucount = counts + (nt + 1);
+    D.vcount = counts + 2 * (nt + 1);
+    D.ucount = counts + 3 * (nt + 1);
+    D.hcursor = counts + 4 * (nt + 1);
+    D.hucursor = D.hcursor + nt;
+    D.vcursor = D.hucursor + nt;
+    D.ucursor = D.vcursor + nt;
+    D.items = D.ucursor + nt;
+    D.home_list = reinterpret_cast<int*>(b + o_home_list);
+    D.visit_list = reinterpret_cast<int*>(b + o_visit);
+    D.n_visit_cap = z.visit_cap;
+    D.home_units = reinterpret_cast<int2*>(b + o_home_units);
+    D.units = reinterpret_cast<int2*>(b + o_units);
+    D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
+    D.n_item_cap = (int)z.item_cap;
+    D.item_units = ITEM_UNITS;
+    D.dense_min = DENSE_MIN;
+    D.dense_blocks_per_sm = 2;
+    D.status = reinterpret_cast<int*>(b + c.o_status);
+    c.scan_tmp = reinterpret_cast<int*>(b + o_scan);
+    return c;
 }
-} // namespace
 } // namespace ibx
 
 // ---------------------------------------------------------------------------
@@ -171,6 +241,8 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
             P.q[c] = P.side ? in.q[c] : static_cast<void*>(static_cast<float*>(in.q[0]) + vol * c);
             P.qi[c] = P.side ? ii.q[c] : static_cast<void*>(static_cast<float*>(ii.q[0]) + vol * c);
         }
+        P.vec4 = P.N[0] % 4 == 0;
+        for (int c = 0; c < ncomp; ++c) P.vec4 = P.vec4 && (reinterpret_cast<unsigned long long>(P.q[c]) & 15) == 0;
         P.tile0 = toffs[p];
         P.marker0 = moffs[p];
         if ((long long)toffs[p] + ntiles > 0x3fffffffLL) return IBX_E_TOO_LARGE;
@@ -179,8 +251,8 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
         visit_cap += (long long)in.n_markers * per;
     }
     if (moffs[n_problems] > 0x7fffffffLL) return IBX_E_TOO_LARGE;
-    const long long item_cap = toffs[n_problems] + visit_cap / ITEM_UNITS + 1;
-    const long long hitem_cap = toffs[n_problems] + moffs[n_problems] / ITEM_UNITS + 1;
+    // Dense work items: at most one per tile plus one per MIN_ITEM_UNITS units.
+    const long long item_cap = toffs[n_problems] + moffs[n_problems] / (MIN_ITEM_UNITS / 3) + 1;
     if (item_cap > 0x7fffffffLL || visit_cap > 0x7fffffffLL) return IBX_E_TOO_LARGE;
     ibx_plan* plan = new (std::nothrow) ibx_plan;
     if (!plan) return IBX_E_OOM;
@@ -190,80 +262,38 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     plan->precision = precision;
     plan->n_probs = n_problems;
     plan->max_ncomp = max_ncomp;
-    const long long nm = moffs[n_problems];
-    const int nt = toffs[n_problems];
+    PlanSizes z;
+    z.n_probs = n_problems;
+    z.n_markers = moffs[n_problems];
+    z.n_tiles = toffs[n_problems];
+    z.visit_cap = visit_cap;
+    z.item_cap = item_cap;
     // One device allocation holds every buffer of the plan.
-    size_t off = 0;
-    auto take = [&](size_t bytes) {
-        const size_t o = off;
-        off = align256(off + bytes);
-        return o;
-    };
-    const size_t o_probs = take(sizeof(PlanProb) * n_problems);
-    const size_t o_moffs = take(sizeof(long long) * (n_problems + 1));
-    const size_t o_toffs = take(sizeof(int) * (n_problems + 1));
-    const size_t o_rec = take(sizeof(Rec) * nm);
-    const size_t o_home_tile = take(sizeof(int) * nm);
-    const size_t o_counts = take(sizeof(int) * counter_ints(nt));
-    const size_t o_item_tile = take(sizeof(int) * item_cap);
-    const size_t o_hitem_tile = take(sizeof(int) * hitem_cap);
-    const size_t o_home_list = take(sizeof(int) * nm);
-    const size_t o_visit = take(sizeof(int) * visit_cap);
-    const size_t o_home_units = take(sizeof(int2) * nm);
-    const size_t o_units = take(sizeof(int2) * visit_cap);
-    const size_t o_status = take(sizeof(int) * 4);
-    const size_t o_scan = take(sizeof(int) * 2048);
+    DevPlan& D = plan->D;
+    const PlanCarve size_only = carve_plan(z, nullptr, D);
     void* dmem = nullptr;
-    if (cudaMalloc(&dmem, off) != cudaSuccess)
+    if (cudaMalloc(&dmem, size_only.bytes) != cudaSuccess)
     {
         delete plan;
         return IBX_E_OOM;
     }
     char* b = static_cast<char*>(dmem);
-    if (cudaMemcpy(b + o_probs, hp.data(), sizeof(PlanProb) * n_problems, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b + o_moffs, moffs.data(), sizeof(long long) * (n_problems + 1), cudaMemcpyHostToDevice) !=
+    const PlanCarve c = carve_plan(z, b, D);
+    if (cudaMemcpy(b + c.o_probs, hp.data(), sizeof(PlanProb) * n_problems, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b + c.o_moffs, moffs.data(), sizeof(long long) * (n_problems + 1), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
-        cudaMemcpy(b + o_toffs, toffs.data(), sizeof(int) * (n_problems + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(b + o_status, 0, sizeof(int) * 4) != cudaSuccess)
+        cudaMemcpy(b + c.o_toffs, toffs.data(), sizeof(int) * (n_problems + 1), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemset(b + c.o_status, 0, sizeof(int) * 4) != cudaSuccess)
     {
         cudaFree(dmem);
         delete plan;
         return IBX_E_CUDA;
     }
-    DevPlan& D = plan->D;
-    D.probs = reinterpret_cast<const PlanProb*>(b + o_probs);
-    D.marker_offs = reinterpret_cast<const long long*>(b + o_moffs);
-    D.tile_offs = reinterpret_cast<const int*>(b + o_toffs);
-    D.n_probs = n_problems;
-    D.n_markers = nm;
-    D.n_tiles = nt;
-    D.rec = reinterpret_cast<Rec*>(b + o_rec);
-    D.home_tile = reinterpret_cast<int*>(b + o_home_tile);
-    int* counts = reinterpret_cast<int*>(b + o_counts);
-    D.hcount = counts;
-    D.vcount = counts + (nt + 1);
-    D.hucount = counts + 2 * (nt + 1);
-    D.ucount = counts + 3 * (nt + 1);
-    D.hcursor = counts + 4 * (nt + 1);
-    D.vcursor = D.hcursor + nt;
-    D.hucursor = D.vcursor + nt;
-    D.ucursor = D.hucursor + nt;
-    D.items = D.ucursor + nt;
-    D.hitems = D.items + (nt + 1);
-    D.hitem_tile = reinterpret_cast<int*>(b + o_hitem_tile);
-    D.n_hitem_cap = (int)hitem_cap;
-    D.home_units = reinterpret_cast<int2*>(b + o_home_units);
-    D.units = reinterpret_cast<int2*>(b + o_units);
-    D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
-    D.n_item_cap = (int)item_cap;
-    D.item_units = ITEM_UNITS;
-    D.home_list = reinterpret_cast<int*>(b + o_home_list);
-    D.visit_list = reinterpret_cast<int*>(b + o_visit);
-    D.n_visit_cap = visit_cap;
-    D.status = reinterpret_cast<int*>(b + o_status);
-    plan->scan_tmp = reinterpret_cast<int*>(b + o_scan);
+    plan->scan_tmp = c.scan_tmp;
+    D.item_units = ITEM_UNITS / max_ncomp;
     plan->dmem = dmem;
-    plan->dbytes = off;
+    plan->dbytes = c.bytes;
     *out = plan;
     return IBX_OK;
 }
@@ -271,26 +301,8 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
 int
 ibx_plan_bin(ibx_plan* plan, void* stream)
 {
-    using namespace ibx;
     if (!plan) return IBX_E_ARG;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    DevPlan& D = plan->D;
-    const int nt = D.n_tiles;
-    // Counters, cursors and item counts are contiguous: one memset.
-    if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
-    int rc = launch_bin(plan->dim, plan->kernel, D, s, false);
-    if (!rc) rc = exclusive_scan(D.hcount, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.hucount, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = exclusive_scan(D.ucount, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = launch_bin(plan->dim, plan->kernel, D, s, true);
-    if (!rc) rc = launch_items(D, s);
-    if (!rc) rc = exclusive_scan(D.items, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = launch_items_fill(D, s);
-    if (!rc) rc = launch_hitems(D, s, false);
-    if (!rc) rc = exclusive_scan(D.hitems, nt + 1, plan->scan_tmp, s);
-    if (!rc) rc = launch_hitems(D, s, true);
-    return rc;
+    return ibx::bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, static_cast<cudaStream_t>(stream));
 }
 
 int
@@ -348,6 +360,31 @@ ibx_plan_status(ibx_plan* plan, void* stream, int* status)
         cudaStreamSynchronize(s) != cudaSuccess || cudaMemsetAsync(plan->D.status, 0, sizeof(int), s) != cudaSuccess)
         return IBX_E_CUDA;
     *status = (word & 1) ? IBX_E_NONFINITE : (word & 2) ? IBX_E_TOO_LARGE : IBX_OK;
+    return IBX_OK;
+}
+
+int
+ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blocks_per_sm)
+{
+    if (!plan) return IBX_E_ARG;
+    if (item_units < ibx::MIN_ITEM_UNITS || item_units > ibx::ITEM_UNITS || dense_min < 0 || dense_blocks_per_sm < 1 ||
+        dense_blocks_per_sm > 32)
+        return IBX_E_ARG;
+    // One thread per (unit, component) in a 256-thread CTA.
+    const int cap = ibx::ITEM_UNITS / plan->max_ncomp;
+    plan->D.item_units = item_units < cap ? item_units : cap;
+    plan->D.dense_min = dense_min;
+    plan->D.dense_blocks_per_sm = dense_blocks_per_sm;
+    return IBX_OK;
+}
+
+int
+ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* dense_blocks_per_sm)
+{
+    if (!plan) return IBX_E_ARG;
+    if (item_units) *item_units = plan->D.item_units;
+    if (dense_min) *dense_min = plan->D.dense_min;
+    if (dense_blocks_per_sm) *dense_blocks_per_sm = plan->D.dense_blocks_per_sm;
     return IBX_OK;
 }
 

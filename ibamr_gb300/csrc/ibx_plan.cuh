@@ -8,9 +8,6 @@ namespace ibx
 {
 constexpr int TILE3 = 8;  // tile edge in 3D (cells)
 constexpr int TILE2 = 16; // tile edge in 2D
-// Tiles with at most this many visits are spread by the warp-per-tile
-// kernel, larger ones by the unit kernel (one CTA per work item).
-constexpr int SPARSE_MAX_VISITS = 96;
 
 template <int DIM>
 struct TileT
@@ -19,7 +16,7 @@ struct TileT
     static constexpr int PTS = DIM == 3 ? E * E * E : E * E;
 };
 
-// Per-marker stencil record (32 bytes).  For every dimension: the stencil
+// Per-marker stencil record (48 bytes).  For every dimension: the stencil
 // base (relative to the box's lower index, shifted by a multiple of N into
 // [0, N) for the cell-centred one) of the cell-centred and of the staggered
 // (side-normal) position, and r_first = t - (base + 1/2), the distance in
@@ -58,6 +55,7 @@ struct PlanProb
     int fixed_ok;      // the fixed-point index path is valid for this problem
     FixedDim fx[3];
     float inv_vol;     // 1/(dx0*dx1[*dx2]) rounded to FP32
+    int vec4;          // N[0] % 4 == 0 and every spread target 16-byte aligned
     const double* X;
     void* Q;           // spread source
     void* q[3];        // spread target, one array per component (side axis or cell depth)
@@ -65,6 +63,11 @@ struct PlanProb
     void* qi[3];       // interpolation source
 };
 
+// Device view of a plan.  Markers whose home tile holds more than dense_min
+// markers ("dense-homed") are spread once each, by their home tile, into a
+// shared-memory region covering the tile and its stencil halo; every other
+// marker is listed once per tile its footprint touches ("visits") and spread
+// by the owner of each visited tile.
 struct DevPlan
 {
     const PlanProb* probs;
@@ -74,19 +77,20 @@ struct DevPlan
     long long n_markers;
     int n_tiles;
     Rec* rec;         // [n_markers], original marker order
+    Rec* hrec;        // [n_markers], home-tile order (same order as home_list)
     int* home_tile;   // [n_markers]
     // Counters (zeroed together each step; the *count arrays are scanned in
-    // place into start offsets).
+    // place into start offsets; hcount/hucount and vcount/ucount are
+    // adjacent so that each pair is scanned by one launch).
     int* hcount;      // [n_tiles+1] markers per home tile
-    int* vcount;      // [n_tiles+1] visits per tile
     int* hucount;     // [n_tiles+1] home units per tile
+    int* vcount;      // [n_tiles+1] visits per tile (sparse-homed markers only)
     int* ucount;      // [n_tiles+1] visit units per tile
     int* hcursor;     // [n_tiles]
-    int* vcursor;     // [n_tiles]
     int* hucursor;    // [n_tiles]
+    int* vcursor;     // [n_tiles]
     int* ucursor;     // [n_tiles]
     int* items;       // [n_tiles+1] dense-tile spread work items, scanned into offsets
-    int* hitems;      // [n_tiles+1] interpolation work items per home tile, scanned
     int* home_list;   // [n_markers] global marker ids grouped by home tile
     int* visit_list;  // [n_visit_cap] global marker ids grouped by visited tile
     long long n_visit_cap;
@@ -96,9 +100,9 @@ struct DevPlan
     int2* units;      // [n_visit_cap]
     int* item_tile;   // [n_item_cap] tile of each work item
     int n_item_cap;
-    int* hitem_tile;  // [n_hitem_cap] home tile of each interpolation work item
-    int n_hitem_cap;
-    int item_units;   // units per spread work item (one per thread)
+    int item_units;   // home units per dense work item (one per thread, <= 256)
+    int dense_min;    // a home tile with more markers than this is dense
+    int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
 
@@ -106,8 +110,34 @@ struct DevPlan
 __host__ __device__ inline size_t
 counter_ints(int n_tiles)
 {
-    return 10 * (size_t)n_tiles + 6;
+    return 9 * (size_t)n_tiles + 5;
 }
+
+// Buffer layout of a plan for the given sizes; with base == nullptr only the
+// byte count is computed.  The problem table, marker and tile offsets are at
+// the returned offsets (to be filled by the caller).
+struct PlanSizes
+{
+    int n_probs;
+    long long n_markers;
+    int n_tiles;
+    long long visit_cap;
+    long long item_cap;
+};
+struct PlanCarve
+{
+    size_t bytes, o_probs, o_moffs, o_toffs, o_status;
+    int* scan_tmp;
+};
+PlanCarve carve_plan(const PlanSizes& z, char* base, DevPlan& D);
+
+// Constants of the exact fixed-point index path for one dimension; false
+// when the problem's coordinate range does not fit it.
+bool fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx);
+
+// The binning sequence of one step (counters zeroed, bin, scans, scatters,
+// dense work items).
+int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s);
 
 template <typename T>
 __device__ __forceinline__ int
@@ -209,11 +239,13 @@ acc2(float* hi, float* lo, float v)
 }
 
 // Launchers (ibx_bin.cu, ibx_spread.cu, ibx_interp.cu).
-int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, bool scatter);
-int exclusive_scan(int* data, int n, int* tmp, cudaStream_t s);
-int launch_items(const DevPlan& D, cudaStream_t s);
-int launch_items_fill(const DevPlan& D, cudaStream_t s);
-int launch_hitems(const DevPlan& D, cudaStream_t s, bool fill);
+// phase 0: bin (records, home counts); 1: home placement and visit counts;
+// 2: visit placement.
+int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase);
+// Exclusive scans of `count` arrays of n ints laid out back to back; tmp
+// holds count * 2048 ints.
+int exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s);
+int launch_items(const DevPlan& D, cudaStream_t s, bool fill);
 int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
 int launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s);
 

@@ -76,6 +76,8 @@ def lib():
             L.ibx_plan_get_bins.argtypes = [ctypes.c_void_p, ip, ip, ip, ip, ip]
             L.ibx_plan_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ip]
             L.ibx_plan_n_tiles.argtypes = [ctypes.c_void_p]
+            L.ibx_plan_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            L.ibx_plan_get_tuning.argtypes = [ctypes.c_void_p, ip, ip, ip]
         _lib = L
     return _lib
 
@@ -218,6 +220,23 @@ class Plan:
         if rc:
             raise IbxError(rc, "ibx_plan_status")
         return st.value
+
+    def set_tuning(self, item_units=None, dense_min=None, dense_blocks_per_sm=None):
+        """Spread tuning knobs (see ibx_plan_set_tuning); None keeps a value."""
+        cur = self.tuning()
+        vals = [cur[0] if item_units is None else item_units, cur[1] if dense_min is None else dense_min,
+                cur[2] if dense_blocks_per_sm is None else dense_blocks_per_sm]
+        rc = lib().ibx_plan_set_tuning(self.h, *[int(v) for v in vals])
+        if rc:
+            raise IbxError(rc, "ibx_plan_set_tuning")
+
+    def tuning(self):
+        """(item_units, dense_min, dense_blocks_per_sm)."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        rc = lib().ibx_plan_get_tuning(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        if rc:
+            raise IbxError(rc, "ibx_plan_get_tuning")
+        return a.value, b.value, c.value
 
     @property
     def n_tiles(self):

@@ -1,0 +1,85 @@
+"""Autotuner of the binned plan's spread.
+
+The spread of a plan has three knobs (``ibx_plan_set_tuning``): the number
+of home units per CTA of the dense-tile kernel (``item_units``, markers per
+block in effect), the home-marker count above which a tile is spread from
+its tile+halo region rather than through per-tile visits (``dense_min``,
+which decides the split between the two kernels), and the CTAs per SM of
+the dense-tile kernel.  The best setting depends on the marker distribution
+(clustered fibres favour regions, scattered markers favour visits), so it
+is measured: every candidate runs ``bin`` + ``spread`` on the plan's own
+data and the fastest is kept.
+
+The tile shape is fixed at compile time (8^3 cells in 3D, 16^2 in 2D).
+
+Tuning spreads into the plan's target arrays (spreading adds), so run it
+before the simulation's first step or on scratch targets.
+"""
+
+import itertools
+
+DEFAULT_CANDIDATES = {
+    "dense_min": (8, 16, 32, 64, 128, 256),
+    "item_units": (32, 64, 128, 256),
+    "dense_blocks_per_sm": (1, 2, 4),
+}
+
+_cache = {}
+
+
+def _time(fn, reps, stream):
+    import torch
+
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
+    """Measure every candidate setting of ``plan`` and keep the fastest.
+
+    Returns {"best": (item_units, dense_min, dense_blocks_per_sm), "ms": t,
+    "table": [((...), ms), ...]}.  With ``key`` the result is cached for
+    this process and later calls with the same key only apply it."""
+    import torch
+
+    if key is not None and key in _cache:
+        plan.set_tuning(*_cache[key]["best"])
+        return _cache[key]
+    cand = dict(DEFAULT_CANDIDATES)
+    if candidates:
+        cand.update(candidates)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        if include_bin:
+            plan.bin()
+        plan.spread()
+
+    table = []
+    # dense_min changes the binning: search it first with the other knobs
+    # at their defaults, then the dense-kernel knobs at the best split.
+    iu0, dm0, bps0 = plan.tuning()
+    for dm in cand["dense_min"]:
+        plan.set_tuning(iu0, dm, bps0)
+        plan.bin()
+        table.append(((iu0, dm, bps0), _time(step, reps, stream)))
+    best_dm = min(table, key=lambda r: r[1])[0][1]
+    for iu, bps in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"]):
+        plan.set_tuning(iu, best_dm, bps)
+        plan.bin()
+        table.append((plan.tuning(), _time(step, reps, stream)))
+    best, ms = min(table, key=lambda r: r[1])
+    plan.set_tuning(*best)
+    plan.bin()
+    out = {"best": best, "ms": ms, "table": table}
+    if key is not None:
+        _cache[key] = out
+    return out

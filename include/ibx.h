@@ -182,6 +182,19 @@ int ibx_plan_get_bins(const ibx_plan* plan, int* base_c, int* base_s, int* home_
                       int* home_list);
 /* Number of tiles of the plan (all problems). */
 int ibx_plan_n_tiles(const ibx_plan* plan);
+
+/* Tuning knobs of a plan's spread (no reference counterpart; set by the
+ * autotuner of the Python package, ibamr_gb300/tuning.py):
+ *   item_units           home units (runs of markers with equal stencil
+ *                        bases) per CTA of the dense-tile kernel, 32..256;
+ *   dense_min            a tile homing more markers than this is spread by
+ *                        the dense-tile kernel (tile + halo region in shared
+ *                        memory), the others by the per-visit kernel;
+ *   dense_blocks_per_sm  CTAs per SM of the dense-tile kernel, 1..32.
+ * Results do not depend on them beyond FP32 rounding.  Takes effect at the
+ * next ibx_plan_bin. */
+int ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blocks_per_sm);
+int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* dense_blocks_per_sm);
 /* Bytes of device scratch the plan holds. */
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);
@@ -196,7 +209,7 @@ int ibx_plan_destroy(ibx_plan* plan);
  *
  * ibx_spread_noalloc: the binned mixed-precision spread of ibx_plan_bin +
  * ibx_plan_spread for one IBX_MODE_PERIODIC problem (float q and Q), with
- * every scratch buffer placed in a fixed 6 MiB array inside the library
+ * every scratch buffer placed in a fixed 8 MiB array inside the library
  * (held on every GPU that loads it until the process exits).  It calls no
  * allocating routine.  Limits: at most IBX_NOALLOC_MAX_MARKERS markers and
  * IBX_NOALLOC_MAX_TILES grid tiles (8^3 cells in 3D, 16^2 in 2D); larger

@@ -34,7 +34,7 @@ def seam_markers(rng, n, dim):
     return X.reshape(-1)
 
 
-def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth):
+def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None):
     ncomp = dim if centering == ibx.SIDE else depth
     shape = list(N)[::-1]
     dx = [1.0 / v for v in N]
@@ -54,6 +54,8 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth):
                                        Q_depth=ncomp)
     ps = ibx.Plan(mk(fq, F_t), kernel, ibx.MIXED)
     pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED)
+    if dense_min is not None:
+        ps.set_tuning(dense_min=dense_min)
     ps.bin()
     ps.spread()
     pi.bin()
@@ -63,10 +65,14 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth):
     return f, U_t.double().cpu().numpy(), ps, pi
 
 
+# dense_min 0: every tile spread by its home region (tile + halo, global
+# atomics); 2^30: every marker spread through its visits (owner
+# read-modify-write); None: the default split.
+@pytest.mark.parametrize("dense_min", [None, 0, 1 << 30])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 1), (0, 3)])
-def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, depth):
+def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, depth, dense_min):
     rng = np.random.default_rng(11 + dim + 100 * centering + 10 * depth + 1000 * KERNEL_NAMES.index(kernel))
     N = [32, 24, 20][:dim] if dim == 3 else [48, 40]
     n = 3000
@@ -75,10 +81,32 @@ def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, dep
     F = rng.standard_normal(n * ncomp)
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
-    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min)
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     assert cases.rel_err(U, U_ref) <= MIXED_TOL
     assert ps.status() == ibx.OK and pi.status() == ibx.OK
+    ps.close()
+    pi.close()
+
+
+@pytest.mark.parametrize("dense_min", [0, 1 << 30])
+@pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "PIECEWISE_LINEAR"])
+@pytest.mark.parametrize("dim,N", [(2, [37, 23]), (3, [19, 13, 11])])
+@pytest.mark.parametrize("centering", [0, 1])
+def test_plan_odd_grid_sizes(ibx, oracle, kernel, dim, N, centering, dense_min):
+    """Grids whose sizes are not multiples of the tile edge or of 4 (partial
+    tiles, scalar row updates, regions wrapping across the periodic seam)."""
+    rng = np.random.default_rng(7 + dim + 31 * centering + (dense_min > 0))
+    n = 1500
+    X = seam_markers(rng, n, dim)
+    ncomp = dim if centering == 1 else 1
+    F = rng.standard_normal(n * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=1)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, 1, dense_min=dense_min)
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(U, U_ref) <= MIXED_TOL
+    assert ps.status() == ibx.OK
     ps.close()
     pi.close()
 
@@ -204,3 +232,37 @@ def test_nonfinite_marker_is_reported_and_skipped(ibx, oracle):
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     ps.close()
     pi.close()
+
+
+def test_autotune_applies_a_measured_setting(ibx, oracle):
+    """The autotuner times every candidate, keeps the fastest, and the tuned
+    plan still matches the oracle (tuning changes the schedule, not the sums
+    beyond FP32 rounding)."""
+    from ibamr_gb300 import tuning
+
+    rng = np.random.default_rng(21)
+    dim, N, kernel = 3, [32, 32, 32], "IB_4"
+    n = 4000
+    X = seam_markers(rng, n, dim)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + N)
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=1)
+    X_t = torch.tensor(X, device="cuda")
+    f_t = [torch.zeros(N, dtype=torch.float32, device="cuda") for _ in range(dim)]
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * 3, [31] * 3, [1 / 32] * 3, [0.0] * 3,
+                                       [1.0] * 3, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED)
+    res = tuning.autotune(plan, reps=1, candidates={"dense_min": (0, 32, 1 << 30), "item_units": (32, 256),
+                                                    "dense_blocks_per_sm": (1, 2)})
+    assert len(res["table"]) == 3 + 4
+    assert plan.tuning() == res["best"]
+    assert res["ms"] == min(t for _, t in res["table"])
+    for t in f_t:
+        t.zero_()
+    plan.bin()
+    plan.spread()
+    torch.cuda.synchronize()
+    f = np.stack([t.double().cpu().numpy() for t in f_t])
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    plan.close()
