@@ -164,6 +164,14 @@ wrap_cell(int c, int N)
 }
 
 // ---- FP32 weights (mixed form) --------------------------------------------
+// sqrt(a) for a > 0 through the hardware reciprocal square root (a few ulp;
+// the mixed form's weights are FP32 values anyway), 0 for a <= 0.
+__device__ __forceinline__ float
+sqrt_f32(float a)
+{
+    return a > 0.f ? a * rsqrtf(a) : 0.f;
+}
+
 __device__ __forceinline__ float
 pcubic_f(float r)
 {
@@ -176,8 +184,8 @@ __device__ __forceinline__ float
 ib3_f(float r)
 {
     r = fabsf(r);
-    if (r < 0.5f) return 0.333333333333333f * (1.f + sqrtf(1.f - 3.f * r * r));
-    if (r < 1.5f) return 0.16666666666667f * (5.f - 3.f * r - sqrtf(1.f - 3.f * (1.f - r) * (1.f - r)));
+    if (r < 0.5f) return 0.333333333333333f * (1.f + sqrt_f32(1.f - 3.f * r * r));
+    if (r < 1.5f) return 0.16666666666667f * (5.f - 3.f * r - sqrt_f32(1.f - 3.f * (1.f - r) * (1.f - r)));
     return 0.f;
 }
 __device__ __forceinline__ float
@@ -201,14 +209,30 @@ weights_f32(float rf, float* w)
     if (K == K_IB4)
     {
         const float r = rf - 1.f;
-        const float q = sqrtf(1.f + 4.f * r * (1.f - r));
+        const float q = sqrt_f32(1.f + 4.f * r * (1.f - r));
         w[0] = 0.125f * (3.f - 2.f * r - q);
         w[1] = 0.125f * (3.f - 2.f * r + q);
         w[2] = 0.125f * (1.f + 2.f * r + q);
         w[3] = 0.125f * (1.f + 2.f * r - q);
     }
     else if (K == K_IB6)
-        ib6_weights<float>(3.f - rf, w);
+    {
+        // The IB_6 quadratic-root weights (ib6_weights) in FP32.
+        const float r = 3.f - rf;
+        const float Kc = 0.714075092976608f;
+        const float r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r6 = r3 * r3;
+        const float beta = (9.f / 4.f) - (3.f / 2.f) * (Kc + r2) + ((22.f / 3.f) - 7.f * Kc) * r - (7.f / 3.f) * r3;
+        const float gamma = 0.25f * (((161.f / 36.f) - (59.f / 6.f) * Kc + 5.f * Kc * Kc) * 0.5f * r2 +
+                                     (-(109.f / 24.f) + 5.f * Kc) * (1.f / 3.f) * r4 + (5.f / 18.f) * r6);
+        const float discr = beta * beta - 112.f * gamma;
+        const float pm3 = (-beta + sqrt_f32(discr)) * (1.f / 56.f);
+        w[0] = pm3;
+        w[1] = -(3.f * pm3) - (1.f / 16.f) + 0.125f * (Kc + r2) + (1.f / 12.f) * (3.f * Kc - 1.f) * r + (1.f / 12.f) * r3;
+        w[2] = 2.f * pm3 + 0.25f + (1.f / 6.f) * (4.f - 3.f * Kc) * r - (1.f / 6.f) * r3;
+        w[3] = 2.f * pm3 + (5.f / 8.f) - 0.25f * (Kc + r2);
+        w[4] = -(3.f * pm3) + 0.25f - (1.f / 6.f) * (4.f - 3.f * Kc) * r + (1.f / 6.f) * r3;
+        w[5] = pm3 - (1.f / 16.f) + 0.125f * (Kc + r2) - (1.f / 12.f) * (3.f * Kc - 1.f) * r - (1.f / 12.f) * r3;
+    }
     else if (K == K_PL)
     {
         w[0] = 1.f - rf;

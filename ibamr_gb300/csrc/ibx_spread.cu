@@ -165,7 +165,9 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
         int org[3];
         tile_origin(P, t - P.tile0, E, DIM, org);
         const int ncomp = P.ncomp;
-        for (int i = threadIdx.x; i < ncomp * 2 * RP; i += blockDim.x) sm[i] = 0.f;
+        for (int i = threadIdx.x; i < ncomp * 2 * RP / 4; i += blockDim.x)
+            reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = ncomp * 2 * RP / 4 * 4 + threadIdx.x; i < ncomp * 2 * RP; i += blockDim.x) sm[i] = 0.f;
         __syncthreads();
         const float* Qf = static_cast<const float*>(P.Q);
         if (RG::regs)
@@ -299,18 +301,43 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
     }
 }
 
-// Visits of sparse-homed markers: one warp per tile, components one after another.  The warp
-// owns a private double-FP32 accumulator for one component of its tile;
-// lanes take visits and merge every contribution with compensated shared
-// atomics (lanes whose footprints overlap are serialised by the atomics);
-// the warp then adds the component to the grid with coalesced FP64 RMWs.
+// Visits of sparse-homed markers: one warp per tile, components one after
+// another.  The warp owns a private double-FP32 accumulator for one
+// component of its tile.  Batches of 32 visits are prepared lane-parallel
+// (weights, and the stencil points that fall inside the tile, compacted per
+// dimension into shared memory); the in-tile points of the whole batch are
+// then numbered consecutively (warp prefix sum) and the lanes take them 32 at
+// a time, each finding its visit by binary search over the batch's first
+// points and merging its contribution with a compensated shared atomic.
+// Finally the warp adds the component to the grid with coalesced
+// read-modify-writes.
+template <int DIM, int W>
+struct VisitSlots
+{
+    static constexpr int SS = DIM * W + 1; // words per visit slot (odd: no bank conflicts)
+    static constexpr int PTS = TileT<DIM>::PTS;
+    // per warp: hi, lo, weights, local indices, counts, values
+    static constexpr int words = 2 * PTS + 2 * 32 * SS + 7 * 32;
+};
+
+// floor(j / n) = (j * magic(n)) >> 16 for 0 <= j < 4096 and 1 <= n <= 6
+// (exact: the error of the fixed-point reciprocal stays below 1/n, the
+// smallest gap between j/n and the next integer).
+__device__ __forceinline__ int
+div_magic(int n)
+{
+    return n == 1 ? 65537 : n == 2 ? 32769 : n == 3 ? 21846 : n == 4 ? 16385 : n == 5 ? 13108 : 10923;
+}
+
 template <int DIM, int K>
 __global__ void __launch_bounds__(32 * SPARSE_WARPS) spread_visits_mixed(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
     constexpr int E = TileT<DIM>::E;
     constexpr int PTS = TileT<DIM>::PTS;
-    extern __shared__ float sm[]; // [SPARSE_WARPS][hi, lo][PTS]
+    using VS = VisitSlots<DIM, W>;
+    constexpr int SS = VS::SS;
+    extern __shared__ float sm[]; // [SPARSE_WARPS][VS::words]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int t = blockIdx.x * SPARSE_WARPS + warp;
     if (t >= D.n_tiles) return;
@@ -321,51 +348,92 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS) spread_visits_mixed(const D
     const PlanProb& P = D.probs[p];
     int org[3];
     tile_origin(P, t - P.tile0, E, DIM, org);
-    float* hi = sm + warp * 2 * PTS;
+    float* hi = sm + warp * VS::words;
     float* lo = hi + PTS;
+    float* wv = lo + PTS;                                  // [32][SS] in-tile weights per dim
+    int* lv = reinterpret_cast<int*>(wv + 32 * SS);       // [32][SS] their local tile indices
+    int* nn = lv + 32 * SS;                                // [3][32] in-tile points per dim
+    int* mg = nn + 3 * 32;                                 // [2][32] division magics of n0, n1
+    int* pf = mg + 2 * 32;                                 // [32] first flattened point of each visit
+    float* Vs = reinterpret_cast<float*>(pf + 32);         // [32] Q / vol
     const float* Qf = static_cast<const float*>(P.Q);
     for (int c = 0; c < P.ncomp; ++c)
     {
-        for (int i = lane; i < 2 * PTS; i += 32) hi[i] = 0.f;
-        __syncwarp();
-        for (int v = vbeg + lane; v < vend; v += 32)
+        for (int i = lane; i < 2 * PTS / 4; i += 32) reinterpret_cast<float4*>(hi)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int b0 = vbeg; b0 < vend; b0 += 32)
         {
-            const int g = D.visit_list[v];
-            const Rec R = D.rec[g];
-            float w[3][W];
-            int b[3] = { 0, 0, 0 };
-#pragma unroll
-            for (int d = 0; d < DIM; ++d)
+            const int v = b0 + lane;
+            int npts = 0;
+            if (v < vend)
             {
-                const bool stag = P.side && d == c;
-                b[d] = stag ? R.bs[d] : R.bc[d];
-                weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
-            }
-            int li[3][W];
-            local_index<DIM, W, E>(b, org, P.N, li);
-            const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
+                const int g = D.visit_list[v];
+                const Rec R = D.rec[g];
+                npts = 1;
 #pragma unroll
-            for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
-            {
-                if (DIM == 3 && li[2][i2] < 0) continue;
-                const float wz = DIM == 3 ? w[2][i2] * V : V;
-                const int zo = DIM == 3 ? li[2][i2] * E * E : 0;
-#pragma unroll
-                for (int i1 = 0; i1 < W; ++i1)
+                for (int d = 0; d < DIM; ++d)
                 {
-                    if (li[1][i1] < 0) continue;
-                    const float wyz = w[1][i1] * wz;
-                    const int row = zo + li[1][i1] * E;
+                    const bool stag = P.side && d == c;
+                    const int b = stag ? R.bs[d] : R.bc[d];
+                    float w[W];
+                    weights_f32<K>(stag ? R.rs[d] : R.rc[d], w);
+                    int n = 0;
 #pragma unroll
-                    for (int i0 = 0; i0 < W; ++i0)
+                    for (int i = 0; i < W; ++i)
                     {
-                        if (li[0][i0] < 0) continue;
-                        acc2(hi + row + li[0][i0], lo + row + li[0][i0], w[0][i0] * wyz);
+                        const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                        if (l >= 0 && l < E)
+                        {
+                            wv[lane * SS + d * W + n] = w[i];
+                            lv[lane * SS + d * W + n] = l;
+                            ++n;
+                        }
                     }
+                    nn[d * 32 + lane] = n;
+                    if (d < 2) mg[d * 32 + lane] = div_magic(n);
+                    npts *= n;
                 }
+                Vs[lane] = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
             }
+            // Exclusive prefix of the visits' in-tile point counts: the
+            // batch's points form one range [0, total) that all lanes share.
+            int incl = npts;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            pf[lane] = incl - npts;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            const int nb = min(32, vend - b0);
+            for (int j = lane; j < total; j += 32)
+            {
+                // the visit holding point j: the last slot whose first point is <= j
+                int kk = 0;
+#pragma unroll
+                for (int st = 16; st >= 1; st >>= 1)
+                    if (kk + st < nb && pf[kk + st] <= j) kk += st;
+                const int jj = j - pf[kk];
+                const int n0 = nn[kk];
+                const int q1 = (jj * mg[kk]) >> 16;
+                const int j0 = jj - q1 * n0;
+                int j1 = q1, j2 = 0;
+                if (DIM == 3)
+                {
+                    const int n1 = nn[32 + kk];
+                    j2 = (q1 * mg[32 + kk]) >> 16;
+                    j1 = q1 - j2 * n1;
+                }
+                const float* ws = wv + kk * SS;
+                const int* ls = lv + kk * SS;
+                const float V = Vs[kk];
+                const float wyz = DIM == 3 ? ws[W + j1] * (ws[2 * W + j2] * V) : ws[W + j1] * V;
+                const int idx = ls[j0] + E * (ls[W + j1] + (DIM == 3 ? E * ls[2 * W + j2] : 0));
+                acc2(hi + idx, lo + idx, ws[j0] * wyz);
+            }
+            __syncwarp();
         }
-        __syncwarp();
         owner_flush<DIM, E, PTS>(P, org, c, hi, lo, lane, 32);
         __syncwarp();
     }
@@ -377,7 +445,7 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
 {
     if (D.n_tiles == 0) return IBX_OK;
     const int pts = dim == 3 ? TileT<3>::PTS : TileT<2>::PTS;
-    const size_t smem_sparse = sizeof(float) * 2 * pts * SPARSE_WARPS;
+    (void)pts;
     const unsigned sparse_blocks = (unsigned)((D.n_tiles + SPARSE_WARPS - 1) / SPARSE_WARPS);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -398,6 +466,7 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
             note_launches(1);                                                                                        \
             if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;                                               \
         }                                                                                                            \
+        const size_t smem_sparse = sizeof(float) * VisitSlots<DD, KT<KK>::W>::words * SPARSE_WARPS;                  \
         if (smem_sparse > 48 * 1024 &&                                                                               \
             cudaFuncSetAttribute(spread_visits_mixed<DD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                  (int)smem_sparse) != cudaSuccess)                                                   \
