@@ -12,6 +12,11 @@ host buffers and the roofline of the dominant kernel are reported on the
 same JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload helices|batched|serving]
+
+--workload batched: 512 independent 2D periodic problems (N uniform in
+{32..512}, 100-20,000 markers each on random closed curves) stepped as one
+CUDA graph; --workload serving: the request loop of ibamr_gb300.serving.
 
 Multi-GPU: replicas only (each rank runs the whole workload on its GPU,
 value = sum over ranks, "scaling": "weak").
@@ -47,6 +52,9 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=float, default=0.1, help="fraction of markers for the CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
+    ap.add_argument("--workload", default="helices", choices=["helices", "batched", "serving"],
+                    help="helices: 2M markers on 256^3 (default); batched: 512 independent 2D problems in one "
+                         "CUDA graph; serving: Poisson request stream over resident simulations")
     return ap.parse_args()
 
 
@@ -372,10 +380,318 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Batched workload: 512 independent 2D periodic problems, one CUDA graph.
+# ---------------------------------------------------------------------------
+BATCH_WORKLOAD = "batched512_2d_N32-512_markers100-20000_fourier_IB4"
+
+
+def batched_problems():
+    from ibamr_gb300 import workloads
+
+    return [([N, N], X) for N, X in workloads.batched_2d(512)]
+
+
+def batched_cpu_baseline(problems, F, n_sample, steps=1, warmup=1):
+    """The per-patch CPU path (oracle port) on a bounded sample of the
+    problems, one problem per host thread; markers/s."""
+    import concurrent.futures
+
+    from oracle import ibx_oracle as oracle
+
+    rng = np.random.default_rng(17)
+    moff = np.concatenate([[0], np.cumsum([X.size // 2 for _, X in problems])])
+    sel = sorted(rng.choice(len(problems), size=min(n_sample, len(problems)), replace=False).tolist())
+    cores = os.cpu_count() or 1
+    work = []
+    for k in sel:
+        N, X = problems[k]
+        vol = N[0] * N[1]
+        Fk = np.ascontiguousarray(F[2 * moff[k]: 2 * moff[k + 1]])
+        u = np.random.default_rng(100 + k).standard_normal(2 * vol)
+        work.append((oracle.CpuPlan(2, N, KERNEL, X, 1), Fk, np.zeros(2 * vol), u, np.zeros(X.size)))
+
+    def run(w):
+        plan, Fk, f, u, U = w
+        plan.step(Fk, f, u, U)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
+        for _ in range(warmup):
+            list(ex.map(run, work))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            list(ex.map(run, work))
+        dt = (time.perf_counter() - t0) / steps
+    m = int(sum(problems[k][1].size // 2 for k in sel))
+    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d problems (%d markers), one problem per thread, %d timed steps"
+                      % (len(sel), len(problems), m, steps), "ms_per_step": dt * 1e3}
+
+
+
+def run_batched(args):
+    import torch
+
+    from ibamr_gb300 import batch, ibx, workloads
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    ibx.lib()
+    problems = batched_problems()
+    B = batch.BatchedProblems(problems, dim=2, kernel=KERNEL, device=dev, tune=not args.no_tune)
+    nm = int(B.marker_offsets[-1])
+    rng = np.random.default_rng(workloads.SEED + 40)
+    F = rng.standard_normal(nm * 2)
+    B.F.copy_(torch.tensor(F, dtype=torch.float32))
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(workloads.SEED + 41)
+    B.u.copy_(torch.randn(B.u.numel(), generator=gen, device=dev))
+    stream = torch.cuda.current_stream()
+
+    # kernels per step, counted on an eager step
+    l0 = ibx.kernel_launches()
+    B.step()
+    per_step = ibx.kernel_launches() - l0
+    B.capture()
+    for _ in range(args.warmup):
+        B.replay()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    barrier()
+    ms = timed(B.replay, args.steps)
+    barrier()
+    clocks = sampler.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nm / (ms * 1e-3)
+
+    reps = max(3, args.steps // 2)
+    t_bin = timed(B.plan.bin, reps)
+    t_spread = timed(B.plan.spread, reps)
+    t_interp = timed(B.plan.interpolate, reps)
+    T = sum(workloads.touched_faces(X, 2, N, KERNEL_W) for N, X in problems)
+    b_spread = nm * 2 * (8 + 4) + T * 2 * 4
+    b_interp = nm * 2 * (8 + 4) + T * 4
+    b_step = nm * 2 * (8 + 8) + T * 3 * 4
+    peak, peak_kind = measured_peak()
+    dom = max([("spread", t_spread, b_spread), ("interpolate", t_interp, b_interp)], key=lambda z: z[1])
+    achieved = (dom[2] / (dom[1] * 1e-3)) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                "step_achieved": (b_step / (ms * 1e-3)) / 1e9, "step_frac": (b_step / (ms * 1e-3)) / 1e9 / peak,
+                "algorithmic_bytes": {"spread": b_spread, "interpolate": b_interp, "step": b_step,
+                                      "touched_faces": T}}
+
+    # accuracy against the plain FP64 form (all 512 problems in one call each)
+    f64 = [[torch.zeros(N[::-1], dtype=torch.float64, device=dev) for _ in range(2)] for N, _ in problems]
+    u64 = [[t.double() for t in B.grid("u", k)] for k in range(len(problems))]
+    F64 = torch.tensor(F, device=dev)
+    U64 = torch.zeros(nm * 2, dtype=torch.float64, device=dev)
+    sp, ip = [], []
+    for k, (N, X) in enumerate(problems):
+        a, b = int(B.marker_offsets[k]) * 2, int(B.marker_offsets[k + 1]) * 2
+        mk = lambda q, Q: ibx.make_problem(2, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [N[0] - 1, N[1] - 1],
+                                           [1.0 / N[0], 1.0 / N[1]], [0.0, 0.0], [1.0, 1.0], q, B.X[a:b], Q[a:b])
+        sp.append(mk(f64[k], F64))
+        ip.append(mk(u64[k], U64))
+
+    def step_plain():
+        ibx.spread(sp, KERNEL, ibx.FP64)
+        ibx.interpolate(ip, KERNEL, ibx.FP64)
+
+    B.f.zero_()
+    B.step()
+    step_plain()
+    torch.cuda.synchronize()
+    err_f = max(float((B.grid("f", k)[a].double() - f64[k][a]).abs().max()) for k in range(len(problems))
+                for a in range(2)) / max(float(f64[k][a].abs().max()) for k in range(len(problems)) for a in range(2))
+    err_U = float((B.U.double() - U64).abs().max() / U64.abs().max())
+    ms_plain = timed(step_plain, max(2, args.steps // 5))
+    del f64, u64
+
+    # end to end: positions and forces in from pinned host memory, velocities out
+    Xh = B.X.cpu().pin_memory()
+    Fh = B.F.cpu().pin_memory()
+    Uh = torch.empty(nm * 2, dtype=torch.float32).pin_memory()
+
+    def step_e2e():
+        B.X.copy_(Xh, non_blocking=True)
+        B.F.copy_(Fh, non_blocking=True)
+        B.replay()
+        Uh.copy_(B.U, non_blocking=True)
+
+    step_e2e()
+    ms_e2e = timed(step_e2e, args.steps)
+    e2e = {"value": world * nm / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nm * 2 * (8 + 4),
+           "d2h_bytes_per_step": nm * 2 * 4, "ms_per_step": ms_e2e}
+    cpu = batched_cpu_baseline(problems, F, 64) if rank == 0 else None
+    tuned = B.tuning
+    B.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
+            "data": "synthetic (seeded)",
+            "config": {"workload": BATCH_WORKLOAD, "problems": len(problems), "markers": nm,
+                       "grid_values": int(sum(2 * N[0] * N[1] for N, _ in problems)), "kernel": KERNEL,
+                       "centering": "side", "precision": "mixed", "launch": "one CUDA graph per step",
+                       "l2": "inputs larger than L2 (2 x 286 MB grids)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
+            "plain_fp64": {"value": nm / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+            "mixed_vs_plain": ms_plain / ms,
+            "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
+            "tuning": None if tuned is None else {
+                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"]))},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# Serving workload: Poisson request stream over resident simulations.
+# ---------------------------------------------------------------------------
+SERVE_WORKLOAD = "serving_poisson2000_32sims_2d64-512_3d32-192_markers1e3-5e5_IB4_budget150GB"
+
+
+def serving_specs(n_sims=32):
+    from ibamr_gb300 import serving, workloads
+
+    rng = np.random.default_rng(workloads.SEED + 5)
+    specs = []
+    for sid in range(n_sims):
+        dim = 2 if rng.uniform() < 0.5 else 3
+        N = int(rng.integers(64, 513)) if dim == 2 else int(rng.integers(32, 193))
+        n = int(np.floor(np.exp(rng.uniform(np.log(1e3), np.log(5e5)))))
+        if dim == 2:
+            X = workloads.fourier_curve(n, 5000 + sid)
+        else:
+            X = workloads.fibonacci_shell(n, N, seed=6000 + sid)
+        F = rng.standard_normal(n * dim)
+        u = rng.standard_normal([dim] + [N] * dim).astype(np.float32)
+        specs.append(serving.SimSpec(sid, dim, [N] * dim, X, F=F, u=u))
+    return specs
+
+
+def serving_cpu_baseline(specs, n_sample=8):
+    """The per-patch CPU path (oracle port) for one request of each of a
+    sample of the simulations, one simulation per host thread; markers/s."""
+    import concurrent.futures
+
+    from oracle import ibx_oracle as oracle
+
+    sel = specs[:n_sample]
+    cores = os.cpu_count() or 1
+    work = []
+    for s in sel:
+        vol = int(np.prod(s.N))
+        work.append((oracle.CpuPlan(s.dim, s.N, KERNEL, s.X, 1), np.ascontiguousarray(s.F, dtype=np.float64),
+                     np.zeros(s.dim * vol), np.ascontiguousarray(s.u, dtype=np.float64).reshape(-1),
+                     np.zeros(s.X.size)))
+
+    def run(w):
+        plan, F, f, u, U = w
+        plan.step(F, f, u, U)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(run, work))
+        t0 = time.perf_counter()
+        list(ex.map(run, work))
+        dt = time.perf_counter() - t0
+    m = int(sum(s.n_markers for s in sel))
+    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "one request of each of %d of %d simulations (%d markers), one simulation per thread"
+                      % (len(sel), len(specs), m), "ms_per_step": dt * 1e3}
+
+
+def run_serving(args):
+    import torch
+
+    from ibamr_gb300 import ibx, serving
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ibx.lib()
+    specs = serving_specs()
+    backend = serving.CudaBackend(KERNEL, device=dev)
+    srv = serving.Server(backend, 150 * 10 ** 9, n_slots=8)
+    for s in specs:
+        srv.register(s)
+    n_req = max(2000, 200 * args.steps)
+    warm = serving.poisson_requests(2000.0, 2 * len(specs), [s.sid for s in specs], seed=1)
+    warm = [serving.Request(i, 0.0, specs[i % len(specs)].sid) for i in range(len(specs))] + warm
+    warm = [serving.Request(i, r.arrival, r.sid) for i, r in enumerate(warm)]
+    srv.run(warm)  # every simulation resident, kernels loaded
+    torch.cuda.synchronize()
+    reqs = serving.poisson_requests(2000.0, n_req, [s.sid for s in specs], seed=2)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    l0 = ibx.kernel_launches()
+    out = srv.run(reqs)
+    torch.cuda.synchronize()
+    launches = ibx.kernel_launches() - l0
+    clocks = sampler.stop()
+    srv.close()
+    cpu = serving_cpu_baseline(specs) if rank == 0 else None
+    if rank == 0:
+        value = world * out["markers_per_s"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_req,
+            "warmup": len(warm), "ms_per_step": out["mean_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
+            "data": "synthetic (seeded)",
+            "config": {"workload": SERVE_WORKLOAD, "simulations": len(specs), "requests": n_req,
+                       "arrival_rate_per_s": 2000.0, "slots": 8, "budget_bytes": 150 * 10 ** 9,
+                       "markers_per_simulation": "log-uniform in [1e3, 5e5]", "kernel": KERNEL,
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "latency_ms": {"p50": out["p50_ms"], "p99": out["p99_ms"], "mean": out["mean_ms"]},
+            "requests_per_s": out["requests_per_s"], "max_queue": out["max_queue"],
+            "resident_bytes": out["used_bytes"], "evictions": out["evictions"],
+            "roofline": None, "cpu_baseline": cpu,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "request loop through the public API; simulation state resident on the device"},
+            "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

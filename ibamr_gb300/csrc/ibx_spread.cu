@@ -339,11 +339,12 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS) spread_visits_mixed(const D
     constexpr int SS = VS::SS;
     extern __shared__ float sm[]; // [SPARSE_WARPS][VS::words]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = blockIdx.x * SPARSE_WARPS + warp;
-    if (t >= D.n_tiles) return;
+    // Persistent: each warp walks tiles with a grid-wide stride.
+    for (int t = blockIdx.x * SPARSE_WARPS + warp; t < D.n_tiles; t += gridDim.x * SPARSE_WARPS)
+    {
     const int vbeg = D.vcount[t];
     const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
-    if (vend <= vbeg) return;
+    if (vend <= vbeg) continue;
     const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
     const PlanProb& P = D.probs[p];
     int org[3];
@@ -437,6 +438,7 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS) spread_visits_mixed(const D
         owner_flush<DIM, E, PTS>(P, org, c, hi, lo, lane, 32);
         __syncwarp();
     }
+    }
 }
 } // namespace
 
@@ -446,7 +448,7 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
     if (D.n_tiles == 0) return IBX_OK;
     const int pts = dim == 3 ? TileT<3>::PTS : TileT<2>::PTS;
     (void)pts;
-    const unsigned sparse_blocks = (unsigned)((D.n_tiles + SPARSE_WARPS - 1) / SPARSE_WARPS);
+    const unsigned sparse_need = (unsigned)((D.n_tiles + SPARSE_WARPS - 1) / SPARSE_WARPS);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -471,6 +473,12 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
             cudaFuncSetAttribute(spread_visits_mixed<DD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
                                  (int)smem_sparse) != cudaSuccess)                                                   \
             return IBX_E_CUDA;                                                                                       \
+        int per_sm_v = 0;                                                                                            \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, spread_visits_mixed<DD, KK>, 32 * SPARSE_WARPS,      \
+                                                      smem_sparse);                                                  \
+        if (per_sm_v < 1) per_sm_v = 1;                                                                              \
+        const unsigned sparse_blocks = sparse_need < (unsigned)(per_sm_v * sms) ? sparse_need                        \
+                                                                               : (unsigned)(per_sm_v * sms);         \
         spread_visits_mixed<DD, KK><<<sparse_blocks, 32 * SPARSE_WARPS, smem_sparse, s>>>(D);                        \
         note_launches(1);                                                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
