@@ -153,10 +153,37 @@ def cpu_baseline(X, F, u_np, fraction, steps=2):
                       % (m, n, N_GRID, cores, steps), "ms_per_step": dt * 1e3}
 
 
+def run_reference_other(args, world):
+    """Reference arm of the batched and serving workloads: the oracle port of
+    the per-patch CPU path over a sample of the same problems."""
+    from ibamr_gb300 import workloads
+
+    if args.workload == "batched":
+        problems = batched_problems()
+        nm = sum(X.size // 2 for _, X in problems)
+        F = np.random.default_rng(workloads.SEED + 40).standard_normal(nm * 2)
+        cpu = batched_cpu_baseline(problems, F, 64, steps=max(1, args.steps // 10), warmup=1)
+        workload = BATCH_WORKLOAD
+    else:
+        cpu = serving_cpu_baseline(serving_specs())
+        workload = SERVE_WORKLOAD
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cpu["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload, "kernel": KERNEL},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
         return
+    if args.workload != "helices":
+        return run_reference_other(args, world)
     X, F = make_markers()
     rng = np.random.default_rng(11)
     u_np = rng.standard_normal(3 * N_GRID ** 3)
@@ -659,8 +686,21 @@ def run_serving(args):
     out = srv.run(reqs)
     torch.cuda.synchronize()
     launches = ibx.kernel_launches() - l0
+    # capacity: the same number of requests all queued at once
+    burst = [serving.Request(r.rid, 0.0, r.sid) for r in reqs[: max(1000, n_req // 2)]]
+    sat = srv.run(burst)
+    torch.cuda.synchronize()
     clocks = sampler.stop()
     srv.close()
+    # algorithmic bytes of one request of each simulation (markers and
+    # touched faces), summed over the saturated run's requests
+    from ibamr_gb300 import workloads
+
+    b_sim = {s.sid: s.n_markers * s.dim * (8 + 8) + 3 * 4 * workloads.touched_faces(s.X, s.dim, s.N, KERNEL_W)
+             for s in specs}
+    span = len(burst) / sat["requests_per_s"]
+    achieved = sum(b_sim[r.sid] for r in burst) / span / 1e9
+    peak, peak_kind = measured_peak()
     cpu = serving_cpu_baseline(specs) if rank == 0 else None
     if rank == 0:
         value = world * out["markers_per_s"]
@@ -676,7 +716,12 @@ def run_serving(args):
             "latency_ms": {"p50": out["p50_ms"], "p99": out["p99_ms"], "mean": out["mean_ms"]},
             "requests_per_s": out["requests_per_s"], "max_queue": out["max_queue"],
             "resident_bytes": out["used_bytes"], "evictions": out["evictions"],
-            "roofline": None, "cpu_baseline": cpu,
+            "saturated": {"requests": len(burst), "markers_per_s": sat["markers_per_s"],
+                          "requests_per_s": sat["requests_per_s"], "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"]},
+            "roofline": {"bound": "hbm", "kernel": "whole request (saturated run)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind},
+            "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                     "note": "request loop through the public API; simulation state resident on the device"},
             "gpu_launches": launches, "clocks": clocks,
