@@ -24,9 +24,12 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_home_mixed(const DevPla
     constexpr int W = KT<K>::W;
     constexpr int NF = DIM == 3 ? W * W * W : W * W;
     constexpr bool CACHE = NF <= 64;
-    const int c = blockIdx.y;
+    // Adjacent threads take the components of one chunk, so that the
+    // chunk's records are read from DRAM once.
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int c = (int)(tid % D.max_ncomp);
     const long long total = D.hcount[D.n_tiles];
-    const long long m0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) * CHUNK;
+    const long long m0 = (tid / D.max_ncomp) * CHUNK;
     if (m0 >= total) return;
     const long long m1 = min(m0 + CHUNK, total);
     float u[CACHE ? NF : 1];
@@ -127,9 +130,9 @@ int
 launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s)
 {
     const long long chunks = (D.n_markers + CHUNK - 1) / CHUNK;
-    const unsigned bx = (unsigned)((chunks + INTERP_THREADS - 1) / INTERP_THREADS);
+    const unsigned bx = (unsigned)((chunks * D.max_ncomp + INTERP_THREADS - 1) / INTERP_THREADS);
     if (bx == 0) return IBX_OK;
-    const dim3 grid(bx, 3);
+    const dim3 grid(bx, 1);
 #define IBX_INTERP_CASE(DD, KK)                                                                                      \
     if (dim == DD && kernel == KK)                                                                                   \
     {                                                                                                                \

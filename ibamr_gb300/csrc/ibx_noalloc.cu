@@ -145,6 +145,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     char* b = static_cast<char*>(base);
     const PlanCarve c = carve_plan(z, b, D);
     D.item_units = 256 / ncomp;
+    D.max_ncomp = ncomp;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const long long moffs[2] = { 0, nm };
     const int toffs[2] = { 0, nt };

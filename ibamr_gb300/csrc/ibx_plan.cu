@@ -292,6 +292,7 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     }
     plan->scan_tmp = c.scan_tmp;
     D.item_units = ITEM_UNITS / max_ncomp;
+    D.max_ncomp = max_ncomp;
     plan->dmem = dmem;
     plan->dbytes = c.bytes;
     *out = plan;

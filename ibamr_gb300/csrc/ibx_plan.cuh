@@ -103,6 +103,7 @@ struct DevPlan
     int item_units;   // home units per dense work item (one per thread, <= 256)
     int dense_min;    // a home tile with more markers than this is dense
     int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
+    int max_ncomp;    // largest component count over the problems
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
 
