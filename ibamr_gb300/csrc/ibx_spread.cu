@@ -193,25 +193,30 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
                     s0[d] = wrap_cell(R0.bc[d] + (W - 1) / 2, P.N[d]) - org[d] + st;
                 }
             }
-            // Markers of the unit, the next one's loads issued before the
-            // current one's arithmetic.
+            // Markers of the unit, software-pipelined: the next marker's
+            // record and value and the id of the one after it are loaded
+            // before the current marker's arithmetic.
             const int vend = un.x + un.y;
+            const long long qstride = P.Q_depth;
+            const float* Qc = Qf + c - qstride * P.marker0;
             Rec Rn;
-            int gn = 0;
+            float Qn = 0.f;
+            int gnn = 0;
             if (un.y > 0)
             {
                 Rn = D.hrec[un.x];
-                gn = D.home_list[un.x];
+                Qn = Qc[qstride * D.home_list[un.x]];
+                if (un.y > 1) gnn = D.home_list[un.x + 1];
             }
             for (int v = un.x; v < vend; ++v)
             {
                 const Rec R = Rn;
-                const int g = gn;
-                const float Qv = Qf[(long long)P.Q_depth * (g - P.marker0) + c];
+                const float Qv = Qn;
                 if (v + 1 < vend)
                 {
                     Rn = D.hrec[v + 1];
-                    gn = D.home_list[v + 1];
+                    Qn = Qc[qstride * gnn];
+                    if (v + 2 < vend) gnn = D.home_list[v + 2];
                 }
                 float w[3][W];
 #pragma unroll
