@@ -81,49 +81,6 @@ merge3(float q, float h, float l)
     return s + (e + l);
 }
 
-// q += hi + lo for every owned value of one component of a tile: lanes take
-// groups of four consecutive x values; rows lying wholly inside the grid
-// are read and written as float4 when the array allows it.
-template <int DIM, int E, int PTS>
-__device__ __forceinline__ void
-owner_flush(const PlanProb& P, const int* org, int c, const float* hi, const float* lo, int tid, int nthr)
-{
-    constexpr int G = PTS / 4;  // groups of 4 values
-    constexpr int GR = E / 4;   // groups per row
-    float* q = static_cast<float*>(P.q[c]);
-    const bool row_vec = P.vec4 && org[0] + E <= P.N[0];
-    for (int j = tid; j < G; j += nthr)
-    {
-        const float4 h = reinterpret_cast<const float4*>(hi)[j];
-        const float4 l = reinterpret_cast<const float4*>(lo)[j];
-        if (h.x == 0.f && h.y == 0.f && h.z == 0.f && h.w == 0.f && l.x == 0.f && l.y == 0.f && l.z == 0.f &&
-            l.w == 0.f)
-            continue;
-        const int r = j / GR;
-        const int x = org[0] + 4 * (j % GR);
-        const int y = org[1] + (DIM == 3 ? r % E : r);
-        const int z = DIM == 3 ? org[2] + r / E : 0;
-        if (y >= P.N[1] || (DIM == 3 && z >= P.N[2])) continue;
-        const long long o = x + (long long)P.N[0] * (y + (long long)P.N[1] * z);
-        if (row_vec)
-        {
-            float4 v = *reinterpret_cast<float4*>(q + o);
-            v.x = merge3(v.x, h.x, l.x);
-            v.y = merge3(v.y, h.y, l.y);
-            v.z = merge3(v.z, h.z, l.z);
-            v.w = merge3(v.w, h.w, l.w);
-            *reinterpret_cast<float4*>(q + o) = v;
-        }
-        else
-        {
-            const float hh[4] = { h.x, h.y, h.z, h.w }, ll[4] = { l.x, l.y, l.z, l.w };
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (x + e < P.N[0] && (hh[e] != 0.f || ll[e] != 0.f)) q[o + e] = merge3(q[o + e], hh[e], ll[e]);
-        }
-    }
-}
-
 // Region sums of one component added to the grid with FP32 atomics.
 template <int DIM, int W>
 __device__ __forceinline__ void
@@ -308,21 +265,32 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
 
 // Visits of sparse-homed markers: one warp per tile, components one after
 // another.  The warp owns a private double-FP32 accumulator for one
-// component of its tile.  Batches of 32 visits are prepared lane-parallel
-// (weights, and the stencil points that fall inside the tile, compacted per
-// dimension into shared memory); the in-tile points of the whole batch are
-// then numbered consecutively (warp prefix sum) and the lanes take them 32 at
-// a time, each finding its visit by binary search over the batch's first
-// points and merging its contribution with a compensated shared atomic.
-// Finally the warp adds the component to the grid with coalesced
-// read-modify-writes.
+// component of its tile, laid out with padded strides so that the 4x4x4 (or
+// 4x4) stencil blocks of a visit fall into distinct shared-memory banks.
+// Batches of 32 visits are prepared lane-parallel: each lane finds the
+// stencil points of its visit that fall inside the tile, and the non-empty
+// visits write their weights and local offsets, compacted per dimension,
+// into consecutive shared-memory slots.  The in-tile points of the batch are
+// numbered consecutively (warp prefix sum) and the lanes take them 32 at a
+// time; a lane finds its visit from one ballot (visits starting at or before
+// the chunk) and one OR-reduction (visits starting inside it), and merges
+// its contribution with a compensated shared atomic.  Finally the warp adds
+// the component to the grid with coalesced read-modify-writes.
+template <int DIM>
+struct TileLayout
+{
+    static constexpr int E = TileT<DIM>::E;
+    static constexpr int RS = DIM == 3 ? E : E + 4;         // row stride (words)
+    static constexpr int PS = DIM == 3 ? E * E + 4 : 0;     // plane stride (words)
+    static constexpr int SZ = DIM == 3 ? E * PS : E * RS;   // words per accumulator
+};
+
 template <int DIM, int W>
 struct VisitSlots
 {
     static constexpr int SS = DIM * W + 1; // words per visit slot (odd: no bank conflicts)
-    static constexpr int PTS = TileT<DIM>::PTS;
-    // per warp: hi, lo, weights, local indices, counts, values
-    static constexpr int words = 2 * PTS + 2 * 32 * SS + 7 * 32;
+    // per warp: hi, lo, slots (weights, local offsets), counts, magics, first points, values
+    static constexpr int words = 2 * TileLayout<DIM>::SZ + 2 * 32 * SS + 7 * 32;
 };
 
 // floor(j / n) = (j * magic(n)) >> 16 for 0 <= j < 4096 and 1 <= n <= 6
@@ -334,115 +302,190 @@ div_magic(int n)
     return n == 1 ? 65537 : n == 2 ? 32769 : n == 3 ? 21846 : n == 4 ? 16385 : n == 5 ? 13108 : 10923;
 }
 
+// q += hi + lo for one component of a tile from the padded accumulator.
+template <int DIM>
+__device__ __forceinline__ void
+tile_flush(const PlanProb& P, const int* org, int c, const float* hi, const float* lo, int lane)
+{
+    using TL = TileLayout<DIM>;
+    constexpr int E = TL::E;
+    constexpr int GR = E / 4; // groups of 4 values per row
+    constexpr int G = (DIM == 3 ? E * E : E) * GR;
+    float* q = static_cast<float*>(P.q[c]);
+    const bool row_vec = P.vec4 && org[0] + E <= P.N[0];
+    for (int j = lane; j < G; j += 32)
+    {
+        const int r = j / GR;
+        const int xo = 4 * (j % GR);
+        const int yl = DIM == 3 ? r % E : r;
+        const int zl = DIM == 3 ? r / E : 0;
+        const int so = xo + yl * TL::RS + zl * TL::PS;
+        const float4 h = *reinterpret_cast<const float4*>(hi + so);
+        const float4 l = *reinterpret_cast<const float4*>(lo + so);
+        if (h.x == 0.f && h.y == 0.f && h.z == 0.f && h.w == 0.f && l.x == 0.f && l.y == 0.f && l.z == 0.f &&
+            l.w == 0.f)
+            continue;
+        const int x = org[0] + xo, y = org[1] + yl, z = org[2] + zl;
+        if (y >= P.N[1] || (DIM == 3 && z >= P.N[2])) continue;
+        const long long o = x + (long long)P.N[0] * (y + (long long)P.N[1] * z);
+        if (row_vec)
+        {
+            float4 v = *reinterpret_cast<float4*>(q + o);
+            v.x = merge3(v.x, h.x, l.x);
+            v.y = merge3(v.y, h.y, l.y);
+            v.z = merge3(v.z, h.z, l.z);
+            v.w = merge3(v.w, h.w, l.w);
+            *reinterpret_cast<float4*>(q + o) = v;
+        }
+        else
+        {
+            const float hh[4] = { h.x, h.y, h.z, h.w }, ll[4] = { l.x, l.y, l.z, l.w };
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (x + e < P.N[0] && (hh[e] != 0.f || ll[e] != 0.f)) q[o + e] = merge3(q[o + e], hh[e], ll[e]);
+        }
+    }
+}
+
 template <int DIM, int K>
-__global__ void __launch_bounds__(32 * SPARSE_WARPS) spread_visits_mixed(const DevPlan D)
+__global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
     constexpr int E = TileT<DIM>::E;
-    constexpr int PTS = TileT<DIM>::PTS;
+    using TL = TileLayout<DIM>;
     using VS = VisitSlots<DIM, W>;
     constexpr int SS = VS::SS;
     extern __shared__ float sm[]; // [SPARSE_WARPS][VS::words]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned le_mask = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;
+    float* hi = sm + warp * VS::words;
+    float* lo = hi + TL::SZ;
+    float* wv = lo + TL::SZ;                          // [32][SS] in-tile weights per dim
+    int* lv = reinterpret_cast<int*>(wv + 32 * SS);  // [32][SS] their offsets in the accumulator
+    int* nn = lv + 32 * SS;                           // [3][32] in-tile points per dim
+    int* mg = nn + 3 * 32;                            // [2][32] division magics of n0, n1
+    int* pf = mg + 2 * 32;                            // [32] first point of each slot
+    float* Vs = reinterpret_cast<float*>(pf + 32);    // [32] Q / vol
     // Persistent: each warp walks tiles with a grid-wide stride.
     for (int t = blockIdx.x * SPARSE_WARPS + warp; t < D.n_tiles; t += gridDim.x * SPARSE_WARPS)
     {
-    const int vbeg = D.vcount[t];
-    const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
-    if (vend <= vbeg) continue;
-    const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
-    const PlanProb& P = D.probs[p];
-    int org[3];
-    tile_origin(P, t - P.tile0, E, DIM, org);
-    float* hi = sm + warp * VS::words;
-    float* lo = hi + PTS;
-    float* wv = lo + PTS;                                  // [32][SS] in-tile weights per dim
-    int* lv = reinterpret_cast<int*>(wv + 32 * SS);       // [32][SS] their local tile indices
-    int* nn = lv + 32 * SS;                                // [3][32] in-tile points per dim
-    int* mg = nn + 3 * 32;                                 // [2][32] division magics of n0, n1
-    int* pf = mg + 2 * 32;                                 // [32] first flattened point of each visit
-    float* Vs = reinterpret_cast<float*>(pf + 32);         // [32] Q / vol
-    const float* Qf = static_cast<const float*>(P.Q);
-    for (int c = 0; c < P.ncomp; ++c)
-    {
-        for (int i = lane; i < 2 * PTS / 4; i += 32) reinterpret_cast<float4*>(hi)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int b0 = vbeg; b0 < vend; b0 += 32)
+        const int vbeg = D.vcount[t];
+        const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
+        if (vend <= vbeg) continue;
+        const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
+        const PlanProb& P = D.probs[p];
+        int org[3];
+        tile_origin(P, t - P.tile0, E, DIM, org);
+        const float* Qf = static_cast<const float*>(P.Q);
+        for (int c = 0; c < P.ncomp; ++c)
         {
-            const int v = b0 + lane;
-            int npts = 0;
-            if (v < vend)
+            for (int i = lane; i < 2 * TL::SZ / 4; i += 32)
+                reinterpret_cast<float4*>(hi)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int b0 = vbeg; b0 < vend; b0 += 32)
             {
-                const int g = D.visit_list[v];
-                const Rec R = D.rec[g];
-                npts = 1;
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
+                // -- lane-parallel preparation of visit b0 + lane ----------
+                const int v = b0 + lane;
+                int cnt[3] = { 1, 1, 1 };
+                unsigned inmask[3] = { 0u, 0u, 0u }; // in-tile stencil points per dim
+                int lof[3][W];
+                float w[3][W];
+                int g = 0;
+                if (v < vend)
                 {
-                    const bool stag = P.side && d == c;
-                    const int b = stag ? R.bs[d] : R.bc[d];
-                    float w[W];
-                    weights_f32<K>(stag ? R.rs[d] : R.rc[d], w);
-                    int n = 0;
+                    g = D.visit_list[v];
+                    const Rec R = D.rec[g];
 #pragma unroll
-                    for (int i = 0; i < W; ++i)
+                    for (int d = 0; d < DIM; ++d)
                     {
-                        const int l = wrap_cell(b + i, P.N[d]) - org[d];
-                        if (l >= 0 && l < E)
+                        const bool stag = P.side && d == c;
+                        const int b = stag ? R.bs[d] : R.bc[d];
+                        weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
+                        const int stride = d == 0 ? 1 : d == 1 ? TL::RS : TL::PS;
+                        int n = 0;
+#pragma unroll
+                        for (int i = 0; i < W; ++i)
                         {
-                            wv[lane * SS + d * W + n] = w[i];
-                            lv[lane * SS + d * W + n] = l;
-                            ++n;
+                            const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                            const bool in = l >= 0 && l < E;
+                            inmask[d] |= in ? (1u << i) : 0u;
+                            n += in ? 1 : 0;
+                            lof[d][i] = l * stride;
                         }
+                        cnt[d] = n;
                     }
-                    nn[d * 32 + lane] = n;
-                    if (d < 2) mg[d * 32 + lane] = div_magic(n);
-                    npts *= n;
                 }
-                Vs[lane] = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
-            }
-            // Exclusive prefix of the visits' in-tile point counts: the
-            // batch's points form one range [0, total) that all lanes share.
-            int incl = npts;
+                const int npts = v < vend ? cnt[0] * cnt[1] * (DIM == 3 ? cnt[2] : 1) : 0;
+                const bool has = npts > 0;
+                const unsigned hm = __ballot_sync(0xffffffffu, has);
+                const int slot = __popc(hm & lt_mask); // compact slot of this visit
+                int incl = npts;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-            {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            pf[lane] = incl - npts;
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            __syncwarp();
-            const int nb = min(32, vend - b0);
-            for (int j = lane; j < total; j += 32)
-            {
-                // the visit holding point j: the last slot whose first point is <= j
-                int kk = 0;
-#pragma unroll
-                for (int st = 16; st >= 1; st >>= 1)
-                    if (kk + st < nb && pf[kk + st] <= j) kk += st;
-                const int jj = j - pf[kk];
-                const int n0 = nn[kk];
-                const int q1 = (jj * mg[kk]) >> 16;
-                const int j0 = jj - q1 * n0;
-                int j1 = q1, j2 = 0;
-                if (DIM == 3)
+                for (int o = 1; o < 32; o <<= 1)
                 {
-                    const int n1 = nn[32 + kk];
-                    j2 = (q1 * mg[32 + kk]) >> 16;
-                    j1 = q1 - j2 * n1;
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
                 }
-                const float* ws = wv + kk * SS;
-                const int* ls = lv + kk * SS;
-                const float V = Vs[kk];
-                const float wyz = DIM == 3 ? ws[W + j1] * (ws[2 * W + j2] * V) : ws[W + j1] * V;
-                const int idx = ls[j0] + E * (ls[W + j1] + (DIM == 3 ? E * ls[2 * W + j2] : 0));
-                acc2(hi + idx, lo + idx, ws[j0] * wyz);
+                const int first = incl - npts;
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                if (has)
+                {
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                    {
+                        int n = 0;
+#pragma unroll
+                        for (int i = 0; i < W; ++i)
+                            if (inmask[d] & (1u << i))
+                            {
+                                wv[slot * SS + d * W + n] = w[d][i];
+                                lv[slot * SS + d * W + n] = lof[d][i];
+                                ++n;
+                            }
+                        nn[d * 32 + slot] = cnt[d];
+                        if (d < 2) mg[d * 32 + slot] = div_magic(cnt[d]);
+                    }
+                    pf[slot] = first;
+                    Vs[slot] = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
+                }
+                __syncwarp();
+                // -- the batch's in-tile points, 32 at a time ---------------
+                for (int base = 0; base < total; base += 32)
+                {
+                    // slot of point base + lane: the non-empty visits that
+                    // start at or before base, plus those starting in
+                    // (base, base + lane]
+                    const int kb = __popc(__ballot_sync(0xffffffffu, has && first <= base)) - 1;
+                    const unsigned starts = __reduce_or_sync(
+                        0xffffffffu, (has && first > base && first < base + 32) ? 1u << (first - base) : 0u);
+                    const int kk = kb + __popc(starts & le_mask);
+                    const int j = base + lane;
+                    if (j < total)
+                    {
+                        const int jj = j - pf[kk];
+                        const int n0 = nn[kk];
+                        const int q1 = (jj * mg[kk]) >> 16;
+                        const int j0 = jj - q1 * n0;
+                        int j1 = q1, j2 = 0;
+                        if (DIM == 3)
+                        {
+                            const int n1 = nn[32 + kk];
+                            j2 = (q1 * mg[32 + kk]) >> 16;
+                            j1 = q1 - j2 * n1;
+                        }
+                        const float* ws = wv + kk * SS;
+                        const int* ls = lv + kk * SS;
+                        const float V = Vs[kk];
+                        const float wyz = DIM == 3 ? ws[W + j1] * (ws[2 * W + j2] * V) : ws[W + j1] * V;
+                        const int idx = ls[j0] + ls[W + j1] + (DIM == 3 ? ls[2 * W + j2] : 0);
+                        acc2(hi + idx, lo + idx, ws[j0] * wyz);
+                    }
+                }
+                __syncwarp();
             }
+            tile_flush<DIM>(P, org, c, hi, lo, lane);
             __syncwarp();
         }
-        owner_flush<DIM, E, PTS>(P, org, c, hi, lo, lane, 32);
-        __syncwarp();
-    }
     }
 }
 } // namespace
