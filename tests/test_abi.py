@@ -33,12 +33,15 @@ def declared_functions():
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = re.sub(r"//[^\n]*", "", text)
         names.update(re.findall(r"\b(ibx_[a-z0-9_]+)\s*\(", text))
+        # the Fortran-ABI routines are declared through IBX_FORTRAN_* macros
+        names.update(re.findall(r"\bIBX_FORTRAN_(?:INTERP|SPREAD)[23]D\((lagrangian_[a-z0-9_]+_)\)", text))
     return sorted(names)
 
 
 def test_every_declared_symbol_is_exported(libibx):
     names = declared_functions()
     assert "ibx_spread" in names and "ibx_plan_create2" in names and "ibx_spread_noalloc" in names
+    assert len([n for n in names if n.startswith("lagrangian_")]) == 24
     out = subprocess.run(["nm", "-D", "--defined-only", libibx], capture_output=True, text=True, check=True).stdout
     exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
     missing = [n for n in names if n not in exported]

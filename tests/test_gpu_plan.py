@@ -266,3 +266,52 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
     f = np.stack([t.double().cpu().numpy() for t in f_t])
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     plan.close()
+
+
+def test_plan_edge_cases_empty_and_boundary_positions(ibx, oracle):
+    """A problem without markers next to one with markers exactly on the
+    periodic boundary (x = 0 and x = 1, the same point), in one plan."""
+    dim, kernel = 2, "IB_4"
+    N = [32, 32]
+    dx = [1.0 / 32] * 2
+    X1 = np.array([0.0, 0.0, 1.0, 1.0, 0.5, 1.0, 1.0, 0.25, 0.999999999999, 1e-300])
+    n1 = X1.size // 2
+    rng = np.random.default_rng(8)
+    F1 = rng.standard_normal(n1 * 2)
+    u1 = rng.standard_normal((2, 32, 32))
+    X1w = np.mod(X1, 1.0)  # the oracle's periodic flow takes positions in [0, 1)
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X1w, F=F1, u=u1)
+    tensors = []
+
+    def prob(X, F, U, f, u):
+        xt = torch.tensor(X, device="cuda")
+        tensors.extend([xt])
+        return (ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [31, 31], dx, [0, 0], [1, 1], f, xt, F,
+                                 n_markers=X.size // 2),
+                ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [31, 31], dx, [0, 0], [1, 1], u, xt, U,
+                                 n_markers=X.size // 2))
+
+    f0 = [torch.zeros(32, 32, dtype=torch.float32, device="cuda") for _ in range(2)]
+    u0 = [torch.zeros(32, 32, dtype=torch.float32, device="cuda") for _ in range(2)]
+    f1 = [torch.zeros(32, 32, dtype=torch.float32, device="cuda") for _ in range(2)]
+    u1t = [torch.tensor(u1[a], dtype=torch.float32, device="cuda") for a in range(2)]
+    e = torch.zeros(2, dtype=torch.float32, device="cuda")
+    F1t = torch.tensor(F1, dtype=torch.float32, device="cuda")
+    U1t = torch.zeros(n1 * 2, dtype=torch.float32, device="cuda")
+    s0, i0 = prob(np.zeros(0), e, e, f0, u0)
+    s1, i1 = prob(X1, F1t, U1t, f1, u1t)
+    for dense_min in (0, 1 << 30):
+        for t in f1:
+            t.zero_()
+        plan = ibx.Plan([s0, s1], kernel, ibx.MIXED, interp_problems=[i0, i1])
+        plan.set_tuning(dense_min=dense_min)
+        plan.bin()
+        plan.spread()
+        plan.interpolate()
+        torch.cuda.synchronize()
+        assert plan.status() == ibx.OK
+        f = np.stack([t.double().cpu().numpy() for t in f1])
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL
+        assert cases.rel_err(U1t.double().cpu().numpy(), U_ref) <= MIXED_TOL
+        assert all(float(t.abs().max()) == 0.0 for t in f0)
+        plan.close()
