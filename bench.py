@@ -249,12 +249,17 @@ def run_ours(args):
         return ibx.make_problem(3, ibx.SIDE, ibx.MODE_PERIODIC, [0] * 3, [N_GRID - 1] * 3, dx, [0.0] * 3, [1.0] * 3,
                                 q, Xq, Q)
 
-    plan = ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)])
+    def make_plan(shape):
+        return ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)],
+                        tile_shape=shape)
+
     tuned = None
-    if not args.no_tune:
+    if args.no_tune:
+        plan = make_plan(0)
+    else:
         from ibamr_gb300 import tuning
 
-        tuned = tuning.autotune(plan)
+        plan, tuned = tuning.autotune_shape(make_plan)
 
     def step():
         plan.bin()
@@ -330,7 +335,7 @@ def run_ours(args):
 
     # ---- accuracy of the mixed form against the plain FP64 form -------------
     f_t2 = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
-    plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED)
+    plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED, tile_shape=plan.tile_shape[0])
     plan_e.set_tuning(*plan.tuning())
     plan_e.bin()
     plan_e.spread()
@@ -381,6 +386,7 @@ def run_ours(args):
            "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e}
 
     cpu = cpu_baseline(X, F, u_np, args.cpu_sample) if rank == 0 else None
+    plan_tile_edges = plan.tile_shape[1]
     plan.close()
     if rank == 0:
         line = {
@@ -396,9 +402,10 @@ def run_ours(args):
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
             "tuning": None if tuned is None else {
+                "tile_shape": tuned["shape"], "tile_edges": list(plan_tile_edges),
                 "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
                 "bin_spread_ms": tuned["ms"],
-                "table": [[list(c), round(t, 4)] for c, t in tuned["table"]]},
+                "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
         }
@@ -594,7 +601,9 @@ def run_batched(args):
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
             "tuning": None if tuned is None else {
-                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"]))},
+                "tile_shape": tuned["shape"],
+                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
+                "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * args.steps,
             "clocks": clocks,
         }

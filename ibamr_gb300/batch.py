@@ -67,13 +67,15 @@ class BatchedProblems:
                                                [0.0] * dim, [1.0] * dim, q, self.X[a:b], Q[a:b])
             sp.append(mk(fq, self.F))
             ip.append(mk(uq, self.U))
-        self.plan = ibx.Plan(sp, kernel, ibx.MIXED, interp_problems=ip)
+        make = lambda shape: ibx.Plan(sp, kernel, ibx.MIXED, interp_problems=ip, tile_shape=shape)
         self.tuning = None
         if tune:
             from . import tuning
 
-            self.tuning = tuning.autotune(self.plan, reps=tune_reps)
+            self.plan, self.tuning = tuning.autotune_shape(make, reps=tune_reps)
             self.f.zero_()
+        else:
+            self.plan = make(0)
         self.graph = None
 
     # -- views ------------------------------------------------------------

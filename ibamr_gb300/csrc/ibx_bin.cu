@@ -158,12 +158,11 @@ tiles_1d(int b, int span, int N, int E, int* out)
     return n;
 }
 
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __device__ __forceinline__ int
 visit_tiles(const PlanProb& P, const Rec& R, int (*tl)[4], int* nt)
 {
     constexpr int W = KT<K>::W;
-    constexpr int E = TileT<DIM>::E;
     int total = 1;
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -176,7 +175,7 @@ visit_tiles(const PlanProb& P, const Rec& R, int (*tl)[4], int* nt)
         }
         const int lo = P.side ? min((int)R.bc[d], (int)R.bs[d]) : R.bc[d];
         const int hi = (P.side ? max((int)R.bc[d], (int)R.bs[d]) : R.bc[d]) + W - 1;
-        nt[d] = tiles_1d(lo, hi - lo + 1, P.N[d], E, tl[d]);
+        nt[d] = tiles_1d(lo, hi - lo + 1, P.N[d], TileT<DIM, SH>::edge(d), tl[d]);
         total *= nt[d];
     }
     return total;
@@ -219,11 +218,10 @@ unit_group(unsigned act, int tile, unsigned long long key)
 // and kernel arguments of the cell-centred and staggered positions) and its
 // home tile, and counts the marker and its unit (warp-local run of markers
 // with equal stencil bases) into the home tile.
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
-    constexpr int E = TileT<DIM>::E;
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     bool valid = g < D.n_markers;
     const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
@@ -264,7 +262,7 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
             R.bs[d] = (short)bs;
             R.rc[d] = rc;
             R.rs[d] = rs;
-            home[d] = wrap_cell(bc + (W - 1) / 2, N) / E;
+            home[d] = wrap_cell(bc + (W - 1) / 2, N) / TileT<DIM, SH>::edge(d);
         }
         if (!finite)
         {
@@ -321,7 +319,7 @@ dense_home(const DevPlan& D, int ht)
 
 // Phase 1: counting sort by home tile (home list, home units and the records
 // in home order); markers of sparse home tiles count their visits.
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
 {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -346,7 +344,7 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
             const int pos = place_group(grp, ht, D.hcursor, D.hcount, D.hucursor, D.hucount, D.home_units);
             D.home_list[pos] = (int)g;
             D.hrec[pos] = R;
-            if (!dense_home(D, ht)) nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+            if (!dense_home(D, ht)) nvis = visit_tiles<DIM, K, SH>(P, R, tl, nt);
         }
     }
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
@@ -366,7 +364,7 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
 }
 
 // Phase 2: counting sort of the visits of sparse-homed markers by visited tile.
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
 {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -380,7 +378,7 @@ __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
     if (valid)
     {
         const Rec R = D.rec[g];
-        nvis = visit_tiles<DIM, K>(P, R, tl, nt);
+        nvis = visit_tiles<DIM, K, SH>(P, R, tl, nt);
         key = base_key<DIM>(R);
     }
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
@@ -500,21 +498,35 @@ launch_items(const DevPlan& D, cudaStream_t s, bool fill)
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
+namespace
+{
+template <int DIM, int K, int SH>
+void
+launch_bin_k(const DevPlan& D, cudaStream_t s, int phase, unsigned blocks)
+{
+    if (phase == 0)
+        bin_kernel<DIM, K, SH><<<blocks, 256, 0, s>>>(D);
+    else if (phase == 1)
+        scatter_home_kernel<DIM, K, SH><<<blocks, 256, 0, s>>>(D);
+    else
+        scatter_visits_kernel<DIM, K, SH><<<blocks, 256, 0, s>>>(D);
+    note_launches(1);
+}
+} // namespace
+
 int
 launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 {
     const unsigned blocks = (unsigned)((D.n_markers + 255) / 256);
     if (blocks == 0) return IBX_OK;
+    const int sh = D.tile_shape;
 #define IBX_BIN_CASE(DD, KK)                                                                                         \
     if (dim == DD && kernel == KK)                                                                                   \
     {                                                                                                                \
-        if (phase == 0)                                                                                              \
-            bin_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                            \
-        else if (phase == 1)                                                                                         \
-            scatter_home_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                   \
+        if (sh == 0)                                                                                                 \
+            launch_bin_k<DD, KK, 0>(D, s, phase, blocks);                                                            \
         else                                                                                                         \
-            scatter_visits_kernel<DD, KK><<<blocks, 256, 0, s>>>(D);                                                 \
-        note_launches(1);                                                                                            \
+            launch_bin_k<DD, KK, 1>(D, s, phase, blocks);                                                            \
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
     }
     IBX_BIN_CASE(2, K_PL) IBX_BIN_CASE(2, K_PCUBIC) IBX_BIN_CASE(2, K_IB3) IBX_BIN_CASE(2, K_IB4)

@@ -79,7 +79,8 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     const int ncomp = in.centering == IBX_SIDE ? dim : in.q_depth;
     if (ncomp > 3) return IBX_E_TOO_LARGE;
     if ((long long)in.n_markers > NOALLOC_MAX_MARKERS) return IBX_E_TOO_LARGE;
-    const int E = dim == 3 ? TILE3 : TILE2;
+    int Ed[3];
+    tile_edges(dim, 0, Ed);
 
     // Problem descriptor (host side), as ibx_plan_create builds it.
     PlanProb P;
@@ -101,7 +102,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
         }
         P.N[d] = in.iupper[d] - in.ilower[d] + 1;
         if (P.N[d] > 30000) return IBX_E_TOO_LARGE;
-        P.ntile[d] = (P.N[d] + E - 1) / E;
+        P.ntile[d] = (P.N[d] + Ed[d] - 1) / Ed[d];
         ntiles *= P.ntile[d];
         vol *= P.N[d];
         P.dx[d] = chk.dx[d];
@@ -131,6 +132,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     const long long nm = in.n_markers;
     const int nt = (int)ntiles;
     PlanSizes z;
+    z.tile_shape = 0;
     z.n_probs = 1;
     z.n_markers = nm;
     z.n_tiles = nt;

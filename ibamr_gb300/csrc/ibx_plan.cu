@@ -129,6 +129,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.n_item_cap = (int)z.item_cap;
     D.item_units = ITEM_UNITS;
     D.dense_min = DENSE_MIN;
+    D.tile_shape = z.tile_shape;
     D.dense_blocks_per_sm = 2;
     D.status = reinterpret_cast<int*>(b + c.o_status);
     c.scan_tmp = reinterpret_cast<int*>(b + o_scan);
@@ -160,10 +161,18 @@ int
 ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
                  int precision, ibx_plan** out)
 {
+    return ibx_plan_create3(problems, interp_problems, n_problems, kernel, precision, 0, out);
+}
+
+int
+ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
+                 int precision, int tile_shape, ibx_plan** out)
+{
     using namespace ibx;
     if (!out) return IBX_E_ARG;
     *out = nullptr;
     if (!problems || !interp_problems || n_problems < 1) return IBX_E_ARG;
+    if (tile_shape < 0 || tile_shape >= N_TILE_SHAPES) return IBX_E_ARG;
     if (kernel < IBX_KERNEL_PIECEWISE_LINEAR || kernel > IBX_KERNEL_BSPLINE_4) return IBX_E_BAD_KERNEL;
     if (precision != IBX_PRECISION_MIXED) return IBX_E_ARG;
     const int dim = problems[0].dim;
@@ -172,7 +181,9 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     std::vector<int> toffs(n_problems + 1, 0);
     long long visit_cap = 0;
     int max_ncomp = 1;
-    const int E = dim == 3 ? TILE3 : TILE2;
+    if (dim != 2 && dim != 3) return IBX_E_ARG;
+    int Ed[3];
+    tile_edges(dim, tile_shape, Ed);
     for (int p = 0; p < n_problems; ++p)
     {
         const ibx_problem& in = problems[p];
@@ -202,6 +213,7 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
             }
             P.N[d] = in.iupper[d] - in.ilower[d] + 1;
             if (P.N[d] > 30000) return IBX_E_TOO_LARGE; // stencil bases are stored as int16
+            const int E = Ed[d];
             P.ntile[d] = (P.N[d] + E - 1) / E;
             ntiles *= P.ntile[d];
             vol *= P.N[d];
@@ -263,6 +275,7 @@ ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems
     plan->n_probs = n_problems;
     plan->max_ncomp = max_ncomp;
     PlanSizes z;
+    z.tile_shape = tile_shape;
     z.n_probs = n_problems;
     z.n_markers = moffs[n_problems];
     z.n_tiles = toffs[n_problems];
@@ -387,6 +400,14 @@ ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* 
     if (dense_min) *dense_min = plan->D.dense_min;
     if (dense_blocks_per_sm) *dense_blocks_per_sm = plan->D.dense_blocks_per_sm;
     return IBX_OK;
+}
+
+int
+ibx_plan_tile_shape(const ibx_plan* plan, int* edges)
+{
+    if (!plan) return -1;
+    if (edges) ibx::tile_edges(plan->dim, plan->D.tile_shape, edges);
+    return plan->D.tile_shape;
 }
 
 int

@@ -6,15 +6,34 @@
 
 namespace ibx
 {
-constexpr int TILE3 = 8;  // tile edge in 3D (cells)
-constexpr int TILE2 = 16; // tile edge in 2D
+// Tile shapes (cells per dimension), chosen per plan:
+//   shape 0: 8 x 8 x 8 in 3D, 16 x 16 in 2D;
+//   shape 1: 16 x 8 x 8 in 3D, 32 x 16 in 2D (longer x rows, fewer tiles
+//            visited per marker, larger dense-tile regions).
+constexpr int N_TILE_SHAPES = 2;
 
-template <int DIM>
+template <int DIM, int SH>
 struct TileT
 {
-    static constexpr int E = DIM == 3 ? TILE3 : TILE2;
-    static constexpr int PTS = DIM == 3 ? E * E * E : E * E;
+    static constexpr int E0 = DIM == 3 ? (SH == 0 ? 8 : 16) : (SH == 0 ? 16 : 32);
+    static constexpr int E1 = DIM == 3 ? 8 : 16;
+    static constexpr int E2 = DIM == 3 ? 8 : 1;
+    static constexpr int PTS = E0 * E1 * E2;
+    __host__ __device__ static constexpr int
+    edge(int d)
+    {
+        return d == 0 ? E0 : d == 1 ? E1 : E2;
+    }
 };
+
+// Tile edges of a shape at run time (host side).
+inline void
+tile_edges(int dim, int shape, int* e)
+{
+    e[0] = dim == 3 ? (shape == 0 ? 8 : 16) : (shape == 0 ? 16 : 32);
+    e[1] = dim == 3 ? 8 : 16;
+    e[2] = dim == 3 ? 8 : 1;
+}
 
 // Per-marker stencil record (48 bytes).  For every dimension: the stencil
 // base (relative to the box's lower index, shifted by a multiple of N into
@@ -104,6 +123,7 @@ struct DevPlan
     int dense_min;    // a home tile with more markers than this is dense
     int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
     int max_ncomp;    // largest component count over the problems
+    int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
 
@@ -119,6 +139,7 @@ counter_ints(int n_tiles)
 // the returned offsets (to be filled by the caller).
 struct PlanSizes
 {
+    int tile_shape;
     int n_probs;
     long long n_markers;
     int n_tiles;
@@ -265,7 +286,7 @@ acc2(float* hi, float* lo, float v)
 
 // Launchers (ibx_bin.cu, ibx_spread.cu, ibx_interp.cu).
 // phase 0: bin (records, home counts); 1: home placement and visit counts;
-// 2: visit placement.
+// 2: visit placement.  The tile shape is D.tile_shape.
 int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase);
 // Exclusive scans of `count` arrays of n ints laid out back to back; tmp
 // holds count * 2048 ints.

@@ -32,41 +32,31 @@ constexpr int UNIT_THREADS = 256;  // threads (units) per dense work item
 constexpr int SPARSE_WARPS = 8;    // tiles (warps) per CTA of the visit kernel
 
 // Region of a dense home tile: the tile plus the stencil halo of every
-// marker homed in it, (E + W)^d values per component.  The cell-centred
-// footprint of a marker homed in the tile starts at region offset
-// (home cell - tile origin) along each dim, the staggered one 0 or 1 later.
-template <int DIM, int W>
+// marker homed in it, (E_d + W) values along each dim per component.  The
+// cell-centred footprint of a marker homed in the tile starts at region
+// offset (home cell - tile origin) along each dim, the staggered one 0 or 1
+// later.
+template <int DIM, int W, int SH>
 struct Region
 {
-    static constexpr int E = TileT<DIM>::E;
-    static constexpr int RE = E + W;
-    static constexpr int RP = DIM == 3 ? RE * RE * RE : RE * RE;
+    using T = TileT<DIM, SH>;
+    static constexpr int R0 = T::E0 + W;
+    static constexpr int R1 = T::E1 + W;
+    static constexpr int R2 = DIM == 3 ? T::E2 + W : 1;
+    static constexpr int RP = R0 * R1 * R2;
     static constexpr int NF = DIM == 3 ? W * W * W : W * W;
     // Footprints up to 4^3 points are accumulated in registers per unit.
     static constexpr bool regs = NF <= 64;
 };
 
+template <int DIM, int SH>
 __device__ __forceinline__ void
-tile_origin(const PlanProb& P, int lt, int E, int dim, int* org)
+tile_origin(const PlanProb& P, int lt, int* org)
 {
-    org[0] = (lt % P.ntile[0]) * E;
-    org[1] = ((lt / P.ntile[0]) % P.ntile[1]) * E;
-    org[2] = dim == 3 ? (lt / (P.ntile[0] * P.ntile[1])) * E : 0;
-}
-
-// Local tile index of stencil point i along each dim, or -1 outside the tile.
-template <int DIM, int W, int E>
-__device__ __forceinline__ void
-local_index(const int* b, const int* org, const int* N, int (*li)[W])
-{
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-#pragma unroll
-        for (int i = 0; i < W; ++i)
-        {
-            const int l = wrap_cell(b[d] + i, N[d]) - org[d];
-            li[d][i] = (l >= 0 && l < E) ? l : -1;
-        }
+    using T = TileT<DIM, SH>;
+    org[0] = (lt % P.ntile[0]) * T::E0;
+    org[1] = ((lt / P.ntile[0]) % P.ntile[1]) * T::E1;
+    org[2] = DIM == 3 ? (lt / (P.ntile[0] * P.ntile[1])) * T::E2 : 0;
 }
 
 // q + hi + lo rounded to FP32 without FP64 arithmetic (GB300 runs FP64 at a
@@ -82,19 +72,19 @@ merge3(float q, float h, float l)
 }
 
 // Region sums of one component added to the grid with FP32 atomics.
-template <int DIM, int W>
+template <int DIM, int W, int SH>
 __device__ __forceinline__ void
 region_flush(const PlanProb& P, const int* org, int c, const float* hi, const float* lo, int tid, int nthr)
 {
-    using RG = Region<DIM, W>;
+    using RG = Region<DIM, W, SH>;
     float* q = static_cast<float*>(P.q[c]);
     for (int i = tid; i < RG::RP; i += nthr)
     {
         const float h = hi[i], l = lo[i];
         if (h == 0.f && l == 0.f) continue;
-        const int lx = i % RG::RE;
-        const int ly = (i / RG::RE) % RG::RE;
-        const int lz = DIM == 3 ? i / (RG::RE * RG::RE) : 0;
+        const int lx = i % RG::R0;
+        const int ly = (i / RG::R0) % RG::R1;
+        const int lz = DIM == 3 ? i / (RG::R0 * RG::R1) : 0;
         const int x = wrap_cell(org[0] - (W - 1) / 2 + lx, P.N[0]);
         const int y = wrap_cell(org[1] - (W - 1) / 2 + ly, P.N[1]);
         const int z = DIM == 3 ? wrap_cell(org[2] - (W - 1) / 2 + lz, P.N[2]) : 0;
@@ -102,13 +92,13 @@ region_flush(const PlanProb& P, const int* org, int c, const float* hi, const fl
     }
 }
 
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
-    constexpr int E = TileT<DIM>::E;
-    using RG = Region<DIM, W>;
-    constexpr int RE = RG::RE;
+    using RG = Region<DIM, W, SH>;
+    constexpr int R0 = RG::R0;
+    constexpr int R01 = RG::R0 * RG::R1;
     constexpr int RP = RG::RP;
     constexpr int NF = RG::NF;
     extern __shared__ float sm[]; // [ncomp][hi, lo][RP]
@@ -120,7 +110,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
         const PlanProb& P = D.probs[p];
         int org[3];
-        tile_origin(P, t - P.tile0, E, DIM, org);
+        tile_origin<DIM, SH>(P, t - P.tile0, org);
         const int ncomp = P.ncomp;
         for (int i = threadIdx.x; i < ncomp * 2 * RP / 4; i += blockDim.x)
             reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -203,7 +193,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
 #pragma unroll
                     for (int i1 = 0; i1 < W; ++i1)
                     {
-                        const int row = (s0[1] + i1) * RE + (DIM == 3 ? (s0[2] + i2) * RE * RE : 0) + s0[0];
+                        const int row = (s0[1] + i1) * R0 + (DIM == 3 ? (s0[2] + i2) * R01 : 0) + s0[0];
 #pragma unroll
                         for (int i0 = 0; i0 < W; ++i0)
                         {
@@ -248,7 +238,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
                         for (int i1 = 0; i1 < W; ++i1)
                         {
                             const float wyz = w[1][i1] * wz;
-                            const int row = (s0[1] + i1) * RE + (DIM == 3 ? (s0[2] + i2) * RE * RE : 0) + s0[0];
+                            const int row = (s0[1] + i1) * R0 + (DIM == 3 ? (s0[2] + i2) * R01 : 0) + s0[0];
 #pragma unroll
                             for (int i0 = 0; i0 < W; ++i0) acc2(hi + row + i0, lo + row + i0, w[0][i0] * wyz);
                         }
@@ -258,7 +248,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
         }
         __syncthreads();
         for (int c = 0; c < ncomp; ++c)
-            region_flush<DIM, W>(P, org, c, sm + (2 * c) * RP, sm + (2 * c + 1) * RP, threadIdx.x, blockDim.x);
+            region_flush<DIM, W, SH>(P, org, c, sm + (2 * c) * RP, sm + (2 * c + 1) * RP, threadIdx.x, blockDim.x);
         __syncthreads();
     }
 }
@@ -276,21 +266,24 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
 // the chunk) and one OR-reduction (visits starting inside it), and merges
 // its contribution with a compensated shared atomic.  Finally the warp adds
 // the component to the grid with coalesced read-modify-writes.
-template <int DIM>
+// Padded accumulator layout of a tile: row and plane strides chosen so that
+// a 4 x 4 block of rows of two consecutive planes falls into distinct banks.
+template <int DIM, int SH>
 struct TileLayout
 {
-    static constexpr int E = TileT<DIM>::E;
-    static constexpr int RS = DIM == 3 ? E : E + 4;         // row stride (words)
-    static constexpr int PS = DIM == 3 ? E * E + 4 : 0;     // plane stride (words)
-    static constexpr int SZ = DIM == 3 ? E * PS : E * RS;   // words per accumulator
+    using T = TileT<DIM, SH>;
+    static constexpr int RS = DIM == 3 ? (SH == 0 ? 8 : 20) : (SH == 0 ? 20 : 36); // row stride (words)
+    static constexpr int PS = DIM == 3 ? (SH == 0 ? 68 : 176) : 0;                 // plane stride (words)
+    static constexpr int SZ = DIM == 3 ? T::E2 * PS : T::E1 * RS;                   // words per accumulator
+    static_assert(RS >= T::E0 && (DIM == 2 || PS >= T::E1 * RS), "padded strides hold a tile");
 };
 
-template <int DIM, int W>
+template <int DIM, int W, int SH>
 struct VisitSlots
 {
     static constexpr int SS = DIM * W + 1; // words per visit slot (odd: no bank conflicts)
     // per warp: hi, lo, slots (weights, local offsets), counts, magics, first points, values
-    static constexpr int words = 2 * TileLayout<DIM>::SZ + 2 * 32 * SS + 7 * 32;
+    static constexpr int words = 2 * TileLayout<DIM, SH>::SZ + 2 * 32 * SS + 7 * 32;
 };
 
 // floor(j / n) = (j * magic(n)) >> 16 for 0 <= j < 4096 and 1 <= n <= 6
@@ -303,22 +296,22 @@ div_magic(int n)
 }
 
 // q += hi + lo for one component of a tile from the padded accumulator.
-template <int DIM>
+template <int DIM, int SH>
 __device__ __forceinline__ void
 tile_flush(const PlanProb& P, const int* org, int c, const float* hi, const float* lo, int lane)
 {
-    using TL = TileLayout<DIM>;
-    constexpr int E = TL::E;
-    constexpr int GR = E / 4; // groups of 4 values per row
-    constexpr int G = (DIM == 3 ? E * E : E) * GR;
+    using TL = TileLayout<DIM, SH>;
+    using T = TileT<DIM, SH>;
+    constexpr int GR = T::E0 / 4; // groups of 4 values per row
+    constexpr int G = T::E1 * T::E2 * GR;
     float* q = static_cast<float*>(P.q[c]);
-    const bool row_vec = P.vec4 && org[0] + E <= P.N[0];
+    const bool row_vec = P.vec4 && org[0] + T::E0 <= P.N[0];
     for (int j = lane; j < G; j += 32)
     {
         const int r = j / GR;
         const int xo = 4 * (j % GR);
-        const int yl = DIM == 3 ? r % E : r;
-        const int zl = DIM == 3 ? r / E : 0;
+        const int yl = r % T::E1;
+        const int zl = r / T::E1;
         const int so = xo + yl * TL::RS + zl * TL::PS;
         const float4 h = *reinterpret_cast<const float4*>(hi + so);
         const float4 l = *reinterpret_cast<const float4*>(lo + so);
@@ -347,13 +340,13 @@ tile_flush(const PlanProb& P, const int* org, int c, const float* hi, const floa
     }
 }
 
-template <int DIM, int K>
+template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
-    constexpr int E = TileT<DIM>::E;
-    using TL = TileLayout<DIM>;
-    using VS = VisitSlots<DIM, W>;
+    using T = TileT<DIM, SH>;
+    using TL = TileLayout<DIM, SH>;
+    using VS = VisitSlots<DIM, W, SH>;
     constexpr int SS = VS::SS;
     extern __shared__ float sm[]; // [SPARSE_WARPS][VS::words]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -376,7 +369,7 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
         const PlanProb& P = D.probs[p];
         int org[3];
-        tile_origin(P, t - P.tile0, E, DIM, org);
+        tile_origin<DIM, SH>(P, t - P.tile0, org);
         const float* Qf = static_cast<const float*>(P.Q);
         for (int c = 0; c < P.ncomp; ++c)
         {
@@ -407,7 +400,7 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
                         for (int i = 0; i < W; ++i)
                         {
                             const int l = wrap_cell(b + i, P.N[d]) - org[d];
-                            const bool in = l >= 0 && l < E;
+                            const bool in = l >= 0 && l < T::edge(d);
                             inmask[d] |= in ? (1u << i) : 0u;
                             n += in ? 1 : 0;
                             lof[d][i] = l * stride;
@@ -483,10 +476,47 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
                 }
                 __syncwarp();
             }
-            tile_flush<DIM>(P, org, c, hi, lo, lane);
+            tile_flush<DIM, SH>(P, org, c, hi, lo, lane);
             __syncwarp();
         }
     }
+}
+} // namespace
+
+namespace
+{
+template <int DIM, int K, int SH>
+int
+launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
+{
+    constexpr int W = KT<K>::W;
+    const int per_sm = D.dense_blocks_per_sm > 0 ? D.dense_blocks_per_sm : 2;
+    const unsigned dense_blocks = (unsigned)(D.n_item_cap < per_sm * sms ? D.n_item_cap : per_sm * sms);
+    const size_t smem = sizeof(float) * 2 * Region<DIM, W, SH>::RP * max_ncomp;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(spread_home_mixed<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return IBX_E_CUDA;
+    if (dense_blocks > 0)
+    {
+        spread_home_mixed<DIM, K, SH><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);
+        note_launches(1);
+        if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
+    }
+    const size_t smem_sparse = sizeof(float) * VisitSlots<DIM, W, SH>::words * SPARSE_WARPS;
+    if (smem_sparse > 48 * 1024 &&
+        cudaFuncSetAttribute(spread_visits_mixed<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_sparse) != cudaSuccess)
+        return IBX_E_CUDA;
+    int per_sm_v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, spread_visits_mixed<DIM, K, SH>, 32 * SPARSE_WARPS,
+                                                  smem_sparse);
+    if (per_sm_v < 1) per_sm_v = 1;
+    const unsigned need = (unsigned)((D.n_tiles + SPARSE_WARPS - 1) / SPARSE_WARPS);
+    const unsigned sparse_blocks = need < (unsigned)(per_sm_v * sms) ? need : (unsigned)(per_sm_v * sms);
+    spread_visits_mixed<DIM, K, SH><<<sparse_blocks, 32 * SPARSE_WARPS, smem_sparse, s>>>(D);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 } // namespace
 
@@ -494,43 +524,13 @@ int
 launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s)
 {
     if (D.n_tiles == 0) return IBX_OK;
-    const int pts = dim == 3 ? TileT<3>::PTS : TileT<2>::PTS;
-    (void)pts;
-    const unsigned sparse_need = (unsigned)((D.n_tiles + SPARSE_WARPS - 1) / SPARSE_WARPS);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int per_sm = D.dense_blocks_per_sm > 0 ? D.dense_blocks_per_sm : 2;
-    const unsigned dense_blocks = (unsigned)(D.n_item_cap < per_sm * sms ? D.n_item_cap : per_sm * sms);
+    const int sh = D.tile_shape;
 #define IBX_SPREAD_CASE(DD, KK)                                                                                      \
     if (dim == DD && kernel == KK)                                                                                   \
-    {                                                                                                                \
-        const size_t smem = sizeof(float) * 2 * Region<DD, KT<KK>::W>::RP * max_ncomp;                               \
-        if (smem > 48 * 1024 &&                                                                                      \
-            cudaFuncSetAttribute(spread_home_mixed<DD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
-                                 (int)smem) != cudaSuccess)                                                          \
-            return IBX_E_CUDA;                                                                                       \
-        if (dense_blocks > 0)                                                                                        \
-        {                                                                                                            \
-            spread_home_mixed<DD, KK><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);                                   \
-            note_launches(1);                                                                                        \
-            if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;                                               \
-        }                                                                                                            \
-        const size_t smem_sparse = sizeof(float) * VisitSlots<DD, KT<KK>::W>::words * SPARSE_WARPS;                  \
-        if (smem_sparse > 48 * 1024 &&                                                                               \
-            cudaFuncSetAttribute(spread_visits_mixed<DD, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,           \
-                                 (int)smem_sparse) != cudaSuccess)                                                   \
-            return IBX_E_CUDA;                                                                                       \
-        int per_sm_v = 0;                                                                                            \
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, spread_visits_mixed<DD, KK>, 32 * SPARSE_WARPS,      \
-                                                      smem_sparse);                                                  \
-        if (per_sm_v < 1) per_sm_v = 1;                                                                              \
-        const unsigned sparse_blocks = sparse_need < (unsigned)(per_sm_v * sms) ? sparse_need                        \
-                                                                               : (unsigned)(per_sm_v * sms);         \
-        spread_visits_mixed<DD, KK><<<sparse_blocks, 32 * SPARSE_WARPS, smem_sparse, s>>>(D);                        \
-        note_launches(1);                                                                                            \
-        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;                                             \
-    }
+        return sh == 0 ? launch_spread_k<DD, KK, 0>(D, max_ncomp, s, sms) : launch_spread_k<DD, KK, 1>(D, max_ncomp, s, sms);
     IBX_SPREAD_CASE(2, K_PL) IBX_SPREAD_CASE(2, K_PCUBIC) IBX_SPREAD_CASE(2, K_IB3) IBX_SPREAD_CASE(2, K_IB4)
     IBX_SPREAD_CASE(2, K_IB6) IBX_SPREAD_CASE(2, K_BSPL4) IBX_SPREAD_CASE(3, K_PL) IBX_SPREAD_CASE(3, K_PCUBIC)
     IBX_SPREAD_CASE(3, K_IB3) IBX_SPREAD_CASE(3, K_IB4) IBX_SPREAD_CASE(3, K_IB6) IBX_SPREAD_CASE(3, K_BSPL4)

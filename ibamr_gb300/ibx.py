@@ -67,6 +67,9 @@ def lib():
                                           ctypes.POINTER(ctypes.c_void_p)]
             L.ibx_plan_create2.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_void_p)]
+            L.ibx_plan_create3.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]
+            L.ibx_plan_tile_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
             for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate"):
                 getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
@@ -182,19 +185,19 @@ def interpolate(problems, kernel, precision=FP64, stream=None):
 class Plan:
     """Binned spread/interpolate pipeline over fixed IBX_MODE_PERIODIC problems."""
 
-    def __init__(self, problems, kernel, precision=MIXED, interp_problems=None):
+    def __init__(self, problems, kernel, precision=MIXED, interp_problems=None, tile_shape=0):
         arr, n = _array(problems)
         self._problems = (problems, interp_problems)
         self._arr = arr
         h = ctypes.c_void_p()
         if interp_problems is None:
-            rc = lib().ibx_plan_create(arr, n, kernel_id(kernel), precision, ctypes.byref(h))
+            arr2 = arr
         else:
             arr2, n2 = _array(interp_problems)
             self._arr2 = arr2
             if n2 != n:
-                raise IbxError(E_ARG, "ibx_plan_create2")
-            rc = lib().ibx_plan_create2(arr, arr2, n, kernel_id(kernel), precision, ctypes.byref(h))
+                raise IbxError(E_ARG, "ibx_plan_create3")
+        rc = lib().ibx_plan_create3(arr, arr2, n, kernel_id(kernel), precision, int(tile_shape), ctypes.byref(h))
         if rc:
             raise IbxError(rc, "ibx_plan_create")
         self.h = h
@@ -229,6 +232,13 @@ class Plan:
         rc = lib().ibx_plan_set_tuning(self.h, *[int(v) for v in vals])
         if rc:
             raise IbxError(rc, "ibx_plan_set_tuning")
+
+    @property
+    def tile_shape(self):
+        """(shape id, tile edges per dimension)."""
+        e = (ctypes.c_int * 3)()
+        sh = lib().ibx_plan_tile_shape(self.h, e)
+        return sh, tuple(e)
 
     def tuning(self):
         """(item_units, dense_min, dense_blocks_per_sm)."""

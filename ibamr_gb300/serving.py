@@ -73,20 +73,27 @@ class SimSpec:
 # Backends
 # ---------------------------------------------------------------------------
 class CudaBackend:
-    """Resident simulations on the current CUDA device; one stream per slot."""
+    """Resident simulations on the current CUDA device; one stream per slot.
+    With ``graphs`` each simulation's step is captured into a CUDA graph when
+    it becomes resident and a request replays it (one launch instead of the
+    step's kernels, no per-request host work beyond that)."""
 
-    def __init__(self, kernel="IB_4", device="cuda"):
+    def __init__(self, kernel="IB_4", device="cuda", graphs=True):
         import torch
 
         self.torch = torch
         self.kernel = kernel
         self.device = torch.device(device)
+        self.graphs = graphs
 
     def make_slots(self, n):
         return [self.torch.cuda.Stream(device=self.device) for _ in range(n)]
 
     def create(self, spec):
-        return _CudaSim(spec, self.kernel, self.device)
+        sim = _CudaSim(spec, self.kernel, self.device)
+        if self.graphs:
+            sim.capture()
+        return sim
 
     def launch(self, sim, slot, keep=False):
         """One step of ``sim`` on stream ``slot``; returns (event, results)
@@ -94,7 +101,10 @@ class CudaBackend:
         ``keep`` is set."""
         torch = self.torch
         with torch.cuda.stream(slot):
-            sim.step(slot)
+            if sim.graph is not None:
+                sim.graph.replay()
+            else:
+                sim.step(slot)
             res = None
             if keep:
                 res = (sim.U.clone(), [t.clone() for t in sim.f])
@@ -130,6 +140,7 @@ class _CudaSim:
                                            [0.0] * dim, [1.0] * dim, q, self.X, Q)
         self.plan = ibx.Plan(mk(self.f, self.F), kernel, ibx.MIXED, interp_problems=[mk(self.u, self.U)])
         self.n_markers = spec.n_markers
+        self.graph = None
         # the uploads and fills above ran on the current stream; the steps
         # run on slot streams
         torch.cuda.current_stream().synchronize()
@@ -141,7 +152,24 @@ class _CudaSim:
         self.plan.spread(stream)
         self.plan.interpolate(stream)
 
+    def capture(self):
+        """Capture one step into a CUDA graph (after an eager warm-up)."""
+        import torch
+
+        s = torch.cuda.Stream(device=self.X.device)
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.step(s)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        self.graph = g
+
     def close(self):
+        self.graph = None
         self.plan.close()
 
 

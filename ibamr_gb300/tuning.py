@@ -10,7 +10,10 @@ the dense-tile kernel.  The best setting depends on the marker distribution
 is measured: every candidate runs ``bin`` + ``spread`` on the plan's own
 data and the fastest is kept.
 
-The tile shape is fixed at compile time (8^3 cells in 3D, 16^2 in 2D).
+The tile shape is a property of a plan, chosen when it is created
+(``autotune_shape`` builds one plan per shape, tunes each, and keeps the
+fastest): shape 0 is 8x8x8 cells in 3D and 16x16 in 2D, shape 1 is 16x8x8 and
+32x16 (longer rows, fewer tiles visited per marker, larger regions).
 
 Tuning spreads into the plan's target arrays (spreading adds), so run it
 before the simulation's first step or on scratch targets.
@@ -83,3 +86,22 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     if key is not None:
         _cache[key] = out
     return out
+
+
+def autotune_shape(make_plan, shapes=(0, 1), reps=3, candidates=None):
+    """Create a plan per tile shape with ``make_plan(shape)``, tune each with
+    ``autotune`` and keep the fastest; the other plans are closed.  Returns
+    (plan, {"shape": id, "ms": t, "per_shape": {id: (best knobs, ms)}})."""
+    best_plan, best, per = None, None, {}
+    for sh in shapes:
+        plan = make_plan(sh)
+        res = autotune(plan, reps=reps, candidates=candidates)
+        per[sh] = (res["best"], res["ms"])
+        if best is None or res["ms"] < best["ms"]:
+            if best_plan is not None:
+                best_plan.close()
+            best_plan, best = plan, {"shape": sh, "ms": res["ms"], "best": res["best"]}
+        else:
+            plan.close()
+    best["per_shape"] = per
+    return best_plan, best

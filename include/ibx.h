@@ -164,6 +164,13 @@ int ibx_plan_create(const ibx_problem* problems, int n_problems, int kernel, int
  * same marker positions X (one binning serves both). */
 int ibx_plan_create2(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
                      int precision, ibx_plan** plan);
+/* ibx_plan_create2 with a tile shape (no reference counterpart; chosen by
+ * the autotuner): 0 = 8x8x8 cells in 3D, 16x16 in 2D (the default);
+ * 1 = 16x8x8 in 3D, 32x16 in 2D.  ibx_plan_tile_shape returns the shape id
+ * and, when edges is not NULL, the tile edges per dimension. */
+int ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems, int n_problems, int kernel,
+                     int precision, int tile_shape, ibx_plan** plan);
+int ibx_plan_tile_shape(const ibx_plan* plan, int* edges);
 int ibx_plan_bin(ibx_plan* plan, void* stream);
 int ibx_plan_spread(ibx_plan* plan, void* stream);
 int ibx_plan_interpolate(ibx_plan* plan, void* stream);

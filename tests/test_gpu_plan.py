@@ -34,7 +34,7 @@ def seam_markers(rng, n, dim):
     return X.reshape(-1)
 
 
-def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None):
+def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, tile_shape=0):
     ncomp = dim if centering == ibx.SIDE else depth
     shape = list(N)[::-1]
     dx = [1.0 / v for v in N]
@@ -52,8 +52,8 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None):
     mk = lambda q, Q: ibx.make_problem(dim, centering, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N], dx,
                                        [0.0] * dim, [1.0] * dim, q, X_t, Q, q_depth=1 if centering else depth,
                                        Q_depth=ncomp)
-    ps = ibx.Plan(mk(fq, F_t), kernel, ibx.MIXED)
-    pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED)
+    ps = ibx.Plan(mk(fq, F_t), kernel, ibx.MIXED, tile_shape=tile_shape)
+    pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED, tile_shape=tile_shape)
     if dense_min is not None:
         ps.set_tuning(dense_min=dense_min)
     ps.bin()
@@ -68,11 +68,12 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None):
 # dense_min 0: every tile spread by its home region (tile + halo, global
 # atomics); 2^30: every marker spread through its visits (owner
 # read-modify-write); None: the default split.
+@pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("dense_min", [None, 0, 1 << 30])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 1), (0, 3)])
-def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, depth, dense_min):
+def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, depth, dense_min, tile_shape):
     rng = np.random.default_rng(11 + dim + 100 * centering + 10 * depth + 1000 * KERNEL_NAMES.index(kernel))
     N = [32, 24, 20][:dim] if dim == 3 else [48, 40]
     n = 3000
@@ -81,19 +82,22 @@ def test_plan_mixed_matches_fp64_oracle(ibx, oracle, kernel, dim, centering, dep
     F = rng.standard_normal(n * ncomp)
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
-    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min,
+                            tile_shape=tile_shape)
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     assert cases.rel_err(U, U_ref) <= MIXED_TOL
     assert ps.status() == ibx.OK and pi.status() == ibx.OK
+    assert ps.tile_shape[0] == tile_shape
     ps.close()
     pi.close()
 
 
+@pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("dense_min", [0, 1 << 30])
 @pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "PIECEWISE_LINEAR"])
 @pytest.mark.parametrize("dim,N", [(2, [37, 23]), (3, [19, 13, 11])])
 @pytest.mark.parametrize("centering", [0, 1])
-def test_plan_odd_grid_sizes(ibx, oracle, kernel, dim, N, centering, dense_min):
+def test_plan_odd_grid_sizes(ibx, oracle, kernel, dim, N, centering, dense_min, tile_shape):
     """Grids whose sizes are not multiples of the tile edge or of 4 (partial
     tiles, scalar row updates, regions wrapping across the periodic seam)."""
     rng = np.random.default_rng(7 + dim + 31 * centering + (dense_min > 0))
@@ -103,7 +107,7 @@ def test_plan_odd_grid_sizes(ibx, oracle, kernel, dim, N, centering, dense_min):
     F = rng.standard_normal(n * ncomp)
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=1)
-    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, 1, dense_min=dense_min)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, 1, dense_min=dense_min, tile_shape=tile_shape)
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     assert cases.rel_err(U, U_ref) <= MIXED_TOL
     assert ps.status() == ibx.OK
@@ -145,9 +149,10 @@ def adversarial_positions(rng, dim, N, n):
     return np.stack(cols, axis=1).reshape(-1)
 
 
+@pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
 @pytest.mark.parametrize("dim", [2, 3])
-def test_binning_bit_exact(ibx, oracle, kernel, dim):
+def test_binning_bit_exact(ibx, oracle, kernel, dim, tile_shape):
     rng = np.random.default_rng(5 + dim + 17 * KERNEL_NAMES.index(kernel))
     N = [64, 64, 64][:dim] if dim == 3 else [128, 96]
     n = 4000
@@ -155,7 +160,7 @@ def test_binning_bit_exact(ibx, oracle, kernel, dim):
     n = X.size // dim
     F = np.zeros(n * dim)
     u = np.zeros([dim] + list(N)[::-1])
-    _, _, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, 1, 1)
+    _, _, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, 1, 1, tile_shape=tile_shape)
     bc, bs, ht, ts, hl = ps.bins(n)
     ebc, ebs = expected_bases(oracle, kernel, X, dim, N)
     assert np.array_equal(bc.reshape(n, 3)[:, :dim], ebc[:, :dim])
@@ -315,3 +320,34 @@ def test_plan_edge_cases_empty_and_boundary_positions(ibx, oracle):
         assert cases.rel_err(U1t.double().cpu().numpy(), U_ref) <= MIXED_TOL
         assert all(float(t.abs().max()) == 0.0 for t in f0)
         plan.close()
+
+
+def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
+    from ibamr_gb300 import tuning
+
+    rng = np.random.default_rng(22)
+    dim, N, kernel = 2, [64, 48], "IB_4"
+    n = 3000
+    X = seam_markers(rng, n, dim)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + N[::-1])
+    f_ref, _ = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=1)
+    X_t = torch.tensor(X, device="cuda")
+    f_t = [torch.zeros(N[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    make = lambda sh: ibx.Plan(ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [63, 47],
+                                                [1 / 64, 1 / 48], [0, 0], [1, 1], f_t, X_t, F_t), kernel,
+                               ibx.MIXED, tile_shape=sh)
+    plan, res = tuning.autotune_shape(make, reps=1, candidates={"dense_min": (0, 1 << 30), "item_units": (64,),
+                                                                "dense_blocks_per_sm": (2,)})
+    assert set(res["per_shape"]) == {0, 1}
+    assert plan.tile_shape[0] == res["shape"]
+    assert res["ms"] == min(v[1] for v in res["per_shape"].values())
+    for t in f_t:
+        t.zero_()
+    plan.bin()
+    plan.spread()
+    torch.cuda.synchronize()
+    f = np.stack([t.double().cpu().numpy() for t in f_t])
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    plan.close()

@@ -1,8 +1,8 @@
-"""Serving loop on the GPU: each request's result is the same alone and in a
-mix of overlapping requests for other simulations (within the mixed-form
-tolerance, the sums differing only in the order of FP32 atomics), a result
-matches the oracle, and the admission estimate bounds the plan's real
-scratch memory."""
+"""Serving loop on the GPU: each request's result is the same alone (eager
+launches) and in a mix of overlapping requests for other simulations (CUDA
+graph replays), within the mixed-form tolerance (the sums differ only in the
+order of FP32 atomics); a result matches the oracle, and the admission
+estimate bounds the plan's real scratch memory."""
 
 import numpy as np
 import pytest
@@ -46,7 +46,8 @@ def test_results_alone_equal_results_in_the_mix(serving, oracle):
     specs = make_specs(serving)
     alone = {}
     for s in specs:
-        srv = serving.Server(serving.CudaBackend("IB_4"), 1 << 36, n_slots=1)
+        # alone: eager launches; in the mix below: graph replays
+        srv = serving.Server(serving.CudaBackend("IB_4", graphs=False), 1 << 36, n_slots=1)
         srv.register(s)
         out = srv.run([serving.Request(0, 0.0, s.sid)], keep_results=True)
         torch.cuda.synchronize()
