@@ -146,7 +146,8 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     if (rs) return rs;
     char* b = static_cast<char*>(base);
     const PlanCarve c = carve_plan(z, b, D);
-    D.item_units = 256 / ncomp;
+    D.zsplit = dense_zsplit(dim, kernel_width(kernel));
+    D.item_units = 2 * (256 / (ncomp * D.zsplit)) < 256 ? 2 * (256 / (ncomp * D.zsplit)) : 256;
     D.max_ncomp = ncomp;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const long long moffs[2] = { 0, nm };

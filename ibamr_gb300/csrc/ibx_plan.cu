@@ -18,6 +18,7 @@
 #include "ibx_plan.cuh"
 #include "../../include/ibx.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -304,7 +305,9 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         return IBX_E_CUDA;
     }
     plan->scan_tmp = c.scan_tmp;
-    D.item_units = ITEM_UNITS / max_ncomp;
+    D.zsplit = dense_zsplit(dim, kernel_width(kernel));
+    // two units per thread: the region is zeroed and flushed once per item
+    D.item_units = std::min(ITEM_UNITS, 2 * (ITEM_UNITS / (max_ncomp * D.zsplit)));
     D.max_ncomp = max_ncomp;
     plan->dmem = dmem;
     plan->dbytes = c.bytes;
@@ -384,9 +387,7 @@ ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blo
     if (item_units < ibx::MIN_ITEM_UNITS || item_units > ibx::ITEM_UNITS || dense_min < 0 || dense_blocks_per_sm < 1 ||
         dense_blocks_per_sm > 32)
         return IBX_E_ARG;
-    // One thread per (unit, component) in a 256-thread CTA.
-    const int cap = ibx::ITEM_UNITS / plan->max_ncomp;
-    plan->D.item_units = item_units < cap ? item_units : cap;
+    plan->D.item_units = item_units;
     plan->D.dense_min = dense_min;
     plan->D.dense_blocks_per_sm = dense_blocks_per_sm;
     return IBX_OK;

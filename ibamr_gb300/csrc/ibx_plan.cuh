@@ -26,6 +26,22 @@ struct TileT
     }
 };
 
+// Threads per (unit, component) of the dense-tile spread: a 4 x 4 x 4
+// footprint is split into two z-halves held by adjacent threads (32
+// accumulators each), other footprints are held by one thread.
+__host__ __device__ constexpr int
+dense_zsplit(int dim, int width)
+{
+    return (dim == 3 && width == 4) ? 2 : 1;
+}
+
+// Stencil width of a kernel id (host side).
+inline int
+kernel_width(int kernel)
+{
+    return kernel == K_PL ? 2 : kernel == K_IB3 ? 3 : kernel == K_IB6 ? 6 : 4;
+}
+
 // Tile edges of a shape at run time (host side).
 inline void
 tile_edges(int dim, int shape, int* e)
@@ -123,6 +139,7 @@ struct DevPlan
     int dense_min;    // a home tile with more markers than this is dense
     int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
     int max_ncomp;    // largest component count over the problems
+    int zsplit;       // dense_zsplit(dim, kernel width)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };

@@ -31,6 +31,13 @@ namespace
 constexpr int UNIT_THREADS = 256;  // threads (units) per dense work item
 constexpr int SPARSE_WARPS = 8;    // tiles (warps) per CTA of the visit kernel
 
+// Smallest v >= n with v = r (mod m).
+__host__ __device__ constexpr int
+pad_to(int n, int m, int r)
+{
+    return n + ((r - n % m) % m + m) % m;
+}
+
 // Region of a dense home tile: the tile plus the stencil halo of every
 // marker homed in it, (E_d + W) values along each dim per component.  The
 // cell-centred footprint of a marker homed in the tile starts at region
@@ -45,8 +52,19 @@ struct Region
     static constexpr int R2 = DIM == 3 ? T::E2 + W : 1;
     static constexpr int RP = R0 * R1 * R2;
     static constexpr int NF = DIM == 3 ? W * W * W : W * W;
-    // Footprints up to 4^3 points are accumulated in registers per unit.
+    // Footprints up to 4^3 points are accumulated in registers per unit,
+    // split over ZS threads along z.
     static constexpr bool regs = NF <= 64;
+    static constexpr int ZS = dense_zsplit(DIM, W);
+    static constexpr int NZ = (DIM == 3 ? W : 1) / ZS; // z-planes per thread
+    static constexpr int NA = NZ * W * W;              // accumulators per thread
+    // Padded shared-memory layout: x + R0*y + PSR*z within a component;
+    // the threads of one unit (its components and z-halves) start 4 banks
+    // apart per z-half (with NZ = 2: PSR = 2 mod 32) and 8 banks apart per
+    // component (CSTR = 8 mod 32), so their atomics do not collide.
+    static constexpr int PSR = (DIM == 3 && ZS == 2) ? pad_to(R0 * R1, 32, 2) : R0 * R1;
+    static constexpr int PAD = R2 * PSR;                 // words of one hi (or lo) block
+    static constexpr int CSTR = pad_to(2 * PAD, 32, 8);  // words per component (hi, lo)
 };
 
 template <int DIM, int SH>
@@ -80,11 +98,12 @@ region_flush(const PlanProb& P, const int* org, int c, const float* hi, const fl
     float* q = static_cast<float*>(P.q[c]);
     for (int i = tid; i < RG::RP; i += nthr)
     {
-        const float h = hi[i], l = lo[i];
-        if (h == 0.f && l == 0.f) continue;
         const int lx = i % RG::R0;
         const int ly = (i / RG::R0) % RG::R1;
         const int lz = DIM == 3 ? i / (RG::R0 * RG::R1) : 0;
+        const int so = lx + RG::R0 * ly + RG::PSR * lz;
+        const float h = hi[so], l = lo[so];
+        if (h == 0.f && l == 0.f) continue;
         const int x = wrap_cell(org[0] - (W - 1) / 2 + lx, P.N[0]);
         const int y = wrap_cell(org[1] - (W - 1) / 2 + ly, P.N[1]);
         const int z = DIM == 3 ? wrap_cell(org[2] - (W - 1) / 2 + lz, P.N[2]) : 0;
@@ -92,16 +111,25 @@ region_flush(const PlanProb& P, const int* org, int c, const float* hi, const fl
     }
 }
 
+// CTAs per SM the register budget is cut for: 3D footprints hold 32
+// accumulators per thread, 2D ones 16.
+template <int DIM>
+struct HomeOccupancy
+{
+    static constexpr int value = DIM == 3 ? 3 : 4;
+};
+
 template <int DIM, int K, int SH>
-__global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPlan D)
+__global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) spread_home_mixed(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
     using RG = Region<DIM, W, SH>;
     constexpr int R0 = RG::R0;
-    constexpr int R01 = RG::R0 * RG::R1;
-    constexpr int RP = RG::RP;
+    constexpr int R01 = RG::PSR; // padded plane stride
+    constexpr int PAD = RG::PAD;
+    constexpr int CSTR = RG::CSTR;
     constexpr int NF = RG::NF;
-    extern __shared__ float sm[]; // [ncomp][hi, lo][RP]
+    extern __shared__ float sm[]; // [ncomp][hi, lo][PAD], components CSTR apart
     const int n_items = D.items[D.n_tiles];
     for (int item = blockIdx.x; item < n_items && item < D.n_item_cap; item += gridDim.x)
     {
@@ -112,95 +140,113 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
         int org[3];
         tile_origin<DIM, SH>(P, t - P.tile0, org);
         const int ncomp = P.ncomp;
-        for (int i = threadIdx.x; i < ncomp * 2 * RP / 4; i += blockDim.x)
+        for (int i = threadIdx.x; i < ncomp * CSTR / 4; i += blockDim.x)
             reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int i = ncomp * 2 * RP / 4 * 4 + threadIdx.x; i < ncomp * 2 * RP; i += blockDim.x) sm[i] = 0.f;
+        for (int i = ncomp * CSTR / 4 * 4 + threadIdx.x; i < ncomp * CSTR; i += blockDim.x) sm[i] = 0.f;
         __syncthreads();
         const float* Qf = static_cast<const float*>(P.Q);
         if (RG::regs)
         {
-            // Thread -> (unit, component): the components of a unit sit in
-            // adjacent lanes and read the same records.
+            // Thread -> (unit, z-half, component): the threads of a unit sit
+            // in adjacent lanes and read the same records.  A CTA holds
+            // blockDim / (ncomp * ZS) units at a time and loops over the
+            // item's units in steps of that.
+            constexpr int ZS = RG::ZS, NZ = RG::NZ, NA = RG::NA;
             const int c = threadIdx.x % ncomp;
-            const int ul = threadIdx.x / ncomp;
-            const int u = D.hucount[t] + k * D.item_units + ul;
-            const bool mine = ul < D.item_units && u < D.hucount[t + 1];
-            const int2 un = mine ? D.home_units[u] : make_int2(0, 0);
-            float acc[NF];
-#pragma unroll
-            for (int i = 0; i < NF; ++i) acc[i] = 0.f;
-            int s0[3] = { 0, 0, 0 };
-            if (un.y > 0)
+            const int zh = (threadIdx.x / ncomp) % ZS;
+            const int ustep = blockDim.x / (ncomp * ZS);
+            for (int ul = threadIdx.x / (ncomp * ZS); ul < D.item_units; ul += ustep)
             {
-                const Rec R0 = D.hrec[un.x];
+                const int u = D.hucount[t] + k * D.item_units + ul;
+                if (threadIdx.x >= ustep * ncomp * ZS || u >= D.hucount[t + 1]) break;
+                const int2 un = D.home_units[u];
+                float acc[NA];
 #pragma unroll
-                for (int d = 0; d < DIM; ++d)
+                for (int i = 0; i < NA; ++i) acc[i] = 0.f;
+                int s0[3] = { 0, 0, 0 };
+                if (un.y > 0)
                 {
-                    const int st = (P.side && d == c) ? min(max(R0.bs[d] - R0.bc[d], 0), 1) : 0; // 0 or 1
-                    s0[d] = wrap_cell(R0.bc[d] + (W - 1) / 2, P.N[d]) - org[d] + st;
-                }
-            }
-            // Markers of the unit, software-pipelined: the next marker's
-            // record and value and the id of the one after it are loaded
-            // before the current marker's arithmetic.
-            const int vend = un.x + un.y;
-            const long long qstride = P.Q_depth;
-            const float* Qc = Qf + c - qstride * P.marker0;
-            Rec Rn;
-            float Qn = 0.f;
-            int gnn = 0;
-            if (un.y > 0)
-            {
-                Rn = D.hrec[un.x];
-                Qn = Qc[qstride * D.home_list[un.x]];
-                if (un.y > 1) gnn = D.home_list[un.x + 1];
-            }
-            for (int v = un.x; v < vend; ++v)
-            {
-                const Rec R = Rn;
-                const float Qv = Qn;
-                if (v + 1 < vend)
-                {
-                    Rn = D.hrec[v + 1];
-                    Qn = Qc[qstride * gnn];
-                    if (v + 2 < vend) gnn = D.home_list[v + 2];
-                }
-                float w[3][W];
+                    const Rec R0 = D.hrec[un.x];
 #pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    weights_f32<K>((P.side && d == c) ? R.rs[d] : R.rc[d], w[d]);
-                const float V = Qv * P.inv_vol;
-#pragma unroll
-                for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
-                {
-                    const float wz = DIM == 3 ? w[2][i2] * V : V;
-#pragma unroll
-                    for (int i1 = 0; i1 < W; ++i1)
+                    for (int d = 0; d < DIM; ++d)
                     {
-                        const float wyz = w[1][i1] * wz;
-#pragma unroll
-                        for (int i0 = 0; i0 < W; ++i0)
-                            acc[(i2 * W + i1) * W + i0] = fmaf(w[0][i0], wyz, acc[(i2 * W + i1) * W + i0]);
+                        const int st = (P.side && d == c) ? min(max(R0.bs[d] - R0.bc[d], 0), 1) : 0; // 0 or 1
+                        s0[d] = wrap_cell(R0.bc[d] + (W - 1) / 2, P.N[d]) - org[d] + st;
                     }
                 }
-            }
-            if (un.y > 0)
-            {
-                float* hi = sm + (2 * c) * RP;
-                float* lo = hi + RP;
-#pragma unroll
-                for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
-#pragma unroll
-                    for (int i1 = 0; i1 < W; ++i1)
+                // Markers of the unit, software-pipelined: the next marker's
+                // record and value and the id of the one after it are loaded
+                // before the current marker's arithmetic.
+                const int vend = un.x + un.y;
+                const long long qstride = P.Q_depth;
+                const float* Qc = Qf + c - qstride * P.marker0;
+                Rec Rn;
+                float Qn = 0.f;
+                int gnn = 0;
+                if (un.y > 0)
+                {
+                    Rn = D.hrec[un.x];
+                    Qn = Qc[qstride * D.home_list[un.x]];
+                    if (un.y > 1) gnn = D.home_list[un.x + 1];
+                }
+                for (int v = un.x; v < vend; ++v)
+                {
+                    const Rec R = Rn;
+                    const float Qv = Qn;
+                    if (v + 1 < vend)
                     {
-                        const int row = (s0[1] + i1) * R0 + (DIM == 3 ? (s0[2] + i2) * R01 : 0) + s0[0];
+                        Rn = D.hrec[v + 1];
+                        Qn = Qc[qstride * gnn];
+                        if (v + 2 < vend) gnn = D.home_list[v + 2];
+                    }
+                    float w[3][W];
 #pragma unroll
-                        for (int i0 = 0; i0 < W; ++i0)
+                    for (int d = 0; d < DIM; ++d)
+                        weights_f32<K>((P.side && d == c) ? R.rs[d] : R.rc[d], w[d]);
+                    const float V = Qv * P.inv_vol;
+                    // this thread's z-planes (selected without dynamic indexing)
+                    float wzv[NZ];
+#pragma unroll
+                    for (int j2 = 0; j2 < NZ; ++j2)
+                    {
+                        float wz = DIM == 3 ? w[2][j2] : 1.f;
+#pragma unroll
+                        for (int h = 1; h < ZS; ++h)
+                            if (zh == h) wz = w[2][h * NZ + j2];
+                        wzv[j2] = wz * V;
+                    }
+#pragma unroll
+                    for (int j2 = 0; j2 < NZ; ++j2)
+                    {
+#pragma unroll
+                        for (int i1 = 0; i1 < W; ++i1)
                         {
-                            const float a = acc[(i2 * W + i1) * W + i0];
-                            if (a != 0.f) acc2(hi + row + i0, lo + row + i0, a);
+                            const float wyz = w[1][i1] * wzv[j2];
+#pragma unroll
+                            for (int i0 = 0; i0 < W; ++i0)
+                                acc[(j2 * W + i1) * W + i0] = fmaf(w[0][i0], wyz, acc[(j2 * W + i1) * W + i0]);
                         }
                     }
+                }
+                if (un.y > 0)
+                {
+                    float* hi = sm + c * CSTR;
+                    float* lo = hi + PAD;
+#pragma unroll
+                    for (int j2 = 0; j2 < NZ; ++j2)
+#pragma unroll
+                        for (int i1 = 0; i1 < W; ++i1)
+                        {
+                            const int row =
+                                (s0[1] + i1) * R0 + (DIM == 3 ? (s0[2] + zh * NZ + j2) * R01 : 0) + s0[0];
+#pragma unroll
+                            for (int i0 = 0; i0 < W; ++i0)
+                            {
+                                const float a = acc[(j2 * W + i1) * W + i0];
+                                if (a != 0.f) acc2(hi + row + i0, lo + row + i0, a);
+                            }
+                        }
+                }
             }
         }
         else
@@ -217,8 +263,8 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
                 const int g = D.home_list[v];
                 for (int c = 0; c < ncomp; ++c)
                 {
-                    float* hi = sm + (2 * c) * RP;
-                    float* lo = hi + RP;
+                    float* hi = sm + c * CSTR;
+                    float* lo = hi + PAD;
                     int s0[3] = { 0, 0, 0 };
                     float w[3][W];
 #pragma unroll
@@ -248,7 +294,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, 2) spread_home_mixed(const DevPl
         }
         __syncthreads();
         for (int c = 0; c < ncomp; ++c)
-            region_flush<DIM, W, SH>(P, org, c, sm + (2 * c) * RP, sm + (2 * c + 1) * RP, threadIdx.x, blockDim.x);
+            region_flush<DIM, W, SH>(P, org, c, sm + c * CSTR, sm + c * CSTR + PAD, threadIdx.x, blockDim.x);
         __syncthreads();
     }
 }
@@ -492,7 +538,7 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
     constexpr int W = KT<K>::W;
     const int per_sm = D.dense_blocks_per_sm > 0 ? D.dense_blocks_per_sm : 2;
     const unsigned dense_blocks = (unsigned)(D.n_item_cap < per_sm * sms ? D.n_item_cap : per_sm * sms);
-    const size_t smem = sizeof(float) * 2 * Region<DIM, W, SH>::RP * max_ncomp;
+    const size_t smem = sizeof(float) * Region<DIM, W, SH>::CSTR * max_ncomp;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(spread_home_mixed<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
