@@ -262,9 +262,7 @@ def run_ours(args):
         plan, tuned = tuning.autotune_shape(make_plan)
 
     def step():
-        plan.bin()
-        plan.spread()
-        plan.interpolate()
+        plan.step()  # bin, then spread and interpolate concurrently
 
     def barrier():
         if world > 1:

@@ -91,10 +91,9 @@ class BatchedProblems:
 
     # -- stepping ----------------------------------------------------------
     def step(self):
-        """bin + spread (f += S F) + interpolate (U = S* u), eagerly."""
-        self.plan.bin()
-        self.plan.spread()
-        self.plan.interpolate()
+        """bin, then spread (f += S F) and interpolate (U = S* u)
+        concurrently, eagerly."""
+        self.plan.step()
 
     def capture(self):
         """Capture one step into a CUDA graph (after an eager warm-up step)."""

@@ -148,6 +148,9 @@ struct ibx_plan
     void* dmem;
     size_t dbytes;
     int* scan_tmp;
+    // ibx_plan_step: interpolation forks onto `side` after the binning
+    cudaStream_t side;
+    cudaEvent_t ev_fork, ev_join;
 };
 
 extern "C" {
@@ -305,6 +308,14 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         return IBX_E_CUDA;
     }
     plan->scan_tmp = c.scan_tmp;
+    if (cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess)
+    {
+        cudaFree(dmem);
+        delete plan;
+        return IBX_E_CUDA;
+    }
     D.zsplit = dense_zsplit(dim, kernel_width(kernel));
     // two units per thread: the region is zeroed and flushed once per item
     D.item_units = std::min(ITEM_UNITS, 2 * (ITEM_UNITS / (max_ncomp * D.zsplit)));
@@ -320,6 +331,26 @@ ibx_plan_bin(ibx_plan* plan, void* stream)
 {
     if (!plan) return IBX_E_ARG;
     return ibx::bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, static_cast<cudaStream_t>(stream));
+}
+
+int
+ibx_plan_step(ibx_plan* plan, void* stream)
+{
+    using namespace ibx;
+    if (!plan) return IBX_E_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s);
+    if (rc) return rc;
+    // spread (stream) and interpolation (side) read the same bins and write
+    // different arrays: they overlap on the device
+    if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
+        return IBX_E_CUDA;
+    rc = launch_interp(plan->dim, plan->kernel, plan->D, plan->side);
+    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
+    // join even after a failed launch, so that the side stream is never left forked
+    if (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess || cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess)
+        return IBX_E_CUDA;
+    return rc ? rc : rs;
 }
 
 int
@@ -427,6 +458,10 @@ int
 ibx_plan_destroy(ibx_plan* plan)
 {
     if (!plan) return IBX_OK;
+    cudaStreamSynchronize(plan->side);
+    cudaStreamDestroy(plan->side);
+    cudaEventDestroy(plan->ev_fork);
+    cudaEventDestroy(plan->ev_join);
     const cudaError_t e = cudaFree(plan->dmem);
     delete plan;
     return e == cudaSuccess ? IBX_OK : IBX_E_CUDA;

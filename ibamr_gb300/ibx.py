@@ -70,7 +70,7 @@ def lib():
             L.ibx_plan_create3.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_void_p)]
             L.ibx_plan_tile_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
-            for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate"):
+            for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate", "ibx_plan_step"):
                 getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.restype = ctypes.c_longlong
@@ -206,6 +206,12 @@ class Plan:
         rc = lib().ibx_plan_bin(self.h, _stream_handle(stream))
         if rc:
             raise IbxError(rc, "ibx_plan_bin")
+
+    def step(self, stream=None):
+        """bin, then spread and interpolate concurrently (ibx_plan_step)."""
+        rc = lib().ibx_plan_step(self.h, _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_plan_step")
 
     def spread(self, stream=None):
         rc = lib().ibx_plan_spread(self.h, _stream_handle(stream))

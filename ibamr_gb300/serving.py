@@ -148,9 +148,7 @@ class _CudaSim:
     def step(self, stream):
         for t in self.f:
             t.zero_()
-        self.plan.bin(stream)
-        self.plan.spread(stream)
-        self.plan.interpolate(stream)
+        self.plan.step(stream)
 
     def capture(self):
         """Capture one step into a CUDA graph (after an eager warm-up)."""

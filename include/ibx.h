@@ -172,6 +172,11 @@ int ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_prob
                      int precision, int tile_shape, ibx_plan** plan);
 int ibx_plan_tile_shape(const ibx_plan* plan, int* edges);
 int ibx_plan_bin(ibx_plan* plan, void* stream);
+/* One whole step: ibx_plan_bin, then ibx_plan_spread on `stream` and
+ * ibx_plan_interpolate on a stream owned by the plan, running concurrently
+ * (they read the same bins and write different arrays), joined back into
+ * `stream` before the call's work ends.  Graph-capturable like the others. */
+int ibx_plan_step(ibx_plan* plan, void* stream);
 int ibx_plan_spread(ibx_plan* plan, void* stream);
 int ibx_plan_interpolate(ibx_plan* plan, void* stream);
 /* Status of the marker data seen by the last ibx_plan_bin (synchronises

@@ -351,3 +351,31 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
     f = np.stack([t.double().cpu().numpy() for t in f_t])
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     plan.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim):
+    """ibx_plan_step (spread and interpolation on two streams) gives the
+    oracle's answer like the separate calls."""
+    rng = np.random.default_rng(61 + dim)
+    N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
+    n = 2500
+    X = seam_markers(rng, n, dim)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, "IB_4", X, F=F, u=u, centering=1)
+    X_t = torch.tensor(X, device="cuda")
+    f_t = [torch.zeros(list(N)[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), "IB_4", ibx.MIXED, interp_problems=[mk(u_t, U_t)])
+    plan.step()
+    torch.cuda.synchronize()
+    f = np.stack([t.double().cpu().numpy() for t in f_t])
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
+    assert plan.status() == ibx.OK
+    plan.close()
