@@ -60,6 +60,8 @@ def lib():
         L.ibx_status_string.argtypes = [ctypes.c_int]
         L.ibx_status_string.restype = ctypes.c_char_p
         L.ibx_kernel_launches.restype = ctypes.c_longlong
+        for name in ("ibx_accumulate_ghosts", "ibx_fill_ghosts"):
+            getattr(L, name).argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
         for name in ("ibx_interpolate", "ibx_spread"):
             getattr(L, name).argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         if hasattr(L, "ibx_plan_create"):
@@ -180,6 +182,23 @@ def interpolate(problems, kernel, precision=FP64, stream=None):
     rc = lib().ibx_interpolate(arr, n, kernel_id(kernel), precision, _stream_handle(stream))
     if rc:
         raise IbxError(rc, "ibx_interpolate")
+
+
+def accumulate_ghosts(problem, periodic, stream=None):
+    """SAMRAIGhostDataAccumulator on one IBX_MODE_PATCH patch covering the
+    domain (ibx_accumulate_ghosts); periodic: per-dimension flags."""
+    per = (ctypes.c_int * 3)(*([int(v) for v in periodic] + [0] * (3 - len(periodic))))
+    rc = lib().ibx_accumulate_ghosts(ctypes.byref(problem), per, _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_accumulate_ghosts")
+
+
+def fill_ghosts(problem, periodic, stream=None):
+    """Periodic ghost fill of one IBX_MODE_PATCH patch covering the domain."""
+    per = (ctypes.c_int * 3)(*([int(v) for v in periodic] + [0] * (3 - len(periodic))))
+    rc = lib().ibx_fill_ghosts(ctypes.byref(problem), per, _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_fill_ghosts")
 
 
 class Plan:

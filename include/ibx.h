@@ -131,6 +131,21 @@ int ibx_interpolate(const ibx_problem* problems, int n_problems, int kernel, int
  * scratch memory; n_problems > 1 as for ibx_interpolate. */
 int ibx_spread(const ibx_problem* problems, int n_problems, int kernel, int precision, void* stream);
 
+/* ---- ghost data of IBX_MODE_PATCH arrays (FP64) ---------------------- */
+/* SAMRAIGhostDataAccumulator::accumulateGhostData
+ * (ibtk/src/math/SAMRAIGhostDataAccumulator.cpp:295-353) for one patch that
+ * covers the whole domain: every value of the ghosted arrays is added into
+ * its degree of freedom (periodic images along dims with periodic[d] != 0;
+ * along other dims positions outside the domain have none and are left as
+ * they are), then every copy of a DOF receives the total (so face N and face
+ * 0 of a periodic side axis hold the same sum).  Sums are taken in array
+ * order, as the reference's vector assembly does. */
+int ibx_accumulate_ghosts(const ibx_problem* problem, const int* periodic, void* stream);
+/* Periodic ghost fill of one patch covering the domain (the periodic copy of
+ * a SAMRAI refine schedule): along dims with periodic[d] != 0 every value
+ * outside the cell box takes the value of its image inside it. */
+int ibx_fill_ghosts(const ibx_problem* problem, const int* periodic, void* stream);
+
 /* ---- host helpers (used by the C++ LEInteractor layer) ----------------- */
 /* Device memory and copies for callers without the CUDA runtime headers:
  * cudaMalloc / cudaFree / blocking cudaMemcpy (to_device != 0: host to
