@@ -60,6 +60,9 @@ def lib():
         L.ibx_status_string.argtypes = [ctypes.c_int]
         L.ibx_status_string.restype = ctypes.c_char_p
         L.ibx_kernel_launches.restype = ctypes.c_longlong
+        L.ibx_spring_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         for name in ("ibx_accumulate_ghosts", "ibx_fill_ghosts"):
             getattr(L, name).argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
         for name in ("ibx_interpolate", "ibx_spread"):
@@ -182,6 +185,24 @@ def interpolate(problems, kernel, precision=FP64, stream=None):
     rc = lib().ibx_interpolate(arr, n, kernel_id(kernel), precision, _stream_handle(stream))
     if rc:
         raise IbxError(rc, "ibx_interpolate")
+
+
+def spring_forces(dim, X, master, slave, stiffness, rest_length, F, accumulate=False, status=None, stream=None):
+    """Linear spring forces into F (ibx_spring_forces).  Device tensors: X
+    float64 (dim per marker), master/slave int32, stiffness/rest_length
+    float64, F float64 (plain form) or float32 (mixed form).  Returns the
+    status tensor (bit 0: a node index was out of range)."""
+    import torch
+
+    if status is None:
+        status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    precision = FP64 if F.dtype == torch.float64 else MIXED
+    rc = lib().ibx_spring_forces(int(dim), int(F.numel() // dim), _ptr(X), int(master.numel()), _ptr(master),
+                                 _ptr(slave), _ptr(stiffness), _ptr(rest_length), _ptr(F), precision,
+                                 1 if accumulate else 0, _ptr(status), _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_spring_forces")
+    return status
 
 
 def accumulate_ghosts(problem, periodic, stream=None):

@@ -146,6 +146,24 @@ int ibx_accumulate_ghosts(const ibx_problem* problem, const int* periodic, void*
  * outside the cell box takes the value of its image inside it. */
 int ibx_fill_ghosts(const ibx_problem* problem, const int* periodic, void* stream);
 
+/* ---- Lagrangian forces before spreading -------------------------------- */
+/* IBStandardForceGen::computeLagrangianSpringForce
+ * (src/IB/IBStandardForceGen.cpp:825-900) with the default linear spring
+ * (include/ibamr/IBSpringForceFunctions.h:104-107), on the device: for spring
+ * k between master[k] and slave[k], D = X_slave - X_master, R = |D|, springs
+ * with R < DBL_EPSILON skipped, T = stiffness[k] * (R - rest_length[k]), and
+ * T/R * D added to F(master) and subtracted from F(slave).  F holds dim
+ * values per marker, double (IBX_PRECISION_FP64) or float (MIXED);
+ * accumulate = 0 zeroes F first.  Node indices outside [0, n_markers) are
+ * skipped and set bit 0 of the device word *status.  All pointers are device
+ * pointers; stream-ordered, so the spread that reads F can follow on the
+ * same stream (or in the same CUDA graph).  Contributions are summed with
+ * atomics: the order of additions, not the values, may differ from the
+ * reference's sequential loop. */
+int ibx_spring_forces(int dim, int n_markers, const double* X, int n_springs, const int* master, const int* slave,
+                      const double* stiffness, const double* rest_length, void* F, int precision, int accumulate,
+                      int* status, void* stream);
+
 /* ---- host helpers (used by the C++ LEInteractor layer) ----------------- */
 /* Device memory and copies for callers without the CUDA runtime headers:
  * cudaMalloc / cudaFree / blocking cudaMemcpy (to_device != 0: host to
