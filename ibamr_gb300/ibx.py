@@ -63,6 +63,8 @@ def lib():
         L.ibx_spring_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.ibx_redistribute.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         for name in ("ibx_accumulate_ghosts", "ibx_fill_ghosts"):
             getattr(L, name).argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
         for name in ("ibx_interpolate", "ibx_spread"):
@@ -185,6 +187,36 @@ def interpolate(problems, kernel, precision=FP64, stream=None):
     rc = lib().ibx_interpolate(arr, n, kernel_id(kernel), precision, _stream_handle(stream))
     if rc:
         raise IbxError(rc, "ibx_interpolate")
+
+
+class PatchBox(ctypes.Structure):
+    """ibx_patch_box: one patch of a level (cell box and geometry)."""
+
+    _fields_ = [("ilower", ctypes.c_int * 3), ("iupper", ctypes.c_int * 3), ("x_lower", ctypes.c_double * 3),
+                ("x_upper", ctypes.c_double * 3), ("dx", ctypes.c_double * 3)]
+
+
+def redistribute(dim, boxes, X, stream=None):
+    """Owner patch of every marker and the markers grouped by owner
+    (ibx_redistribute).  boxes: [(ilower, iupper, x_lower, x_upper, dx), ...];
+    X: device float64 tensor.  Returns (owner, order, patch_offsets) device
+    int32 tensors."""
+    import torch
+
+    arr = (PatchBox * max(1, len(boxes)))()
+    for k, (ilo, ihi, xl, xu, dx) in enumerate(boxes):
+        for d in range(dim):
+            arr[k].ilower[d], arr[k].iupper[d] = int(ilo[d]), int(ihi[d])
+            arr[k].x_lower[d], arr[k].x_upper[d], arr[k].dx[d] = float(xl[d]), float(xu[d]), float(dx[d])
+    n = X.numel() // dim
+    owner = torch.empty(n, dtype=torch.int32, device=X.device)
+    order = torch.empty(n, dtype=torch.int32, device=X.device)
+    offsets = torch.empty(len(boxes) + 2, dtype=torch.int32, device=X.device)
+    rc = lib().ibx_redistribute(int(dim), arr, len(boxes), _ptr(X), int(n), _ptr(owner), _ptr(order), _ptr(offsets),
+                                _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_redistribute")
+    return owner, order, offsets
 
 
 def spring_forces(dim, X, master, slave, stiffness, rest_length, F, accumulate=False, status=None, stream=None):

@@ -146,6 +146,29 @@ int ibx_accumulate_ghosts(const ibx_problem* problem, const int* periodic, void*
  * outside the cell box takes the value of its image inside it. */
 int ibx_fill_ghosts(const ibx_problem* problem, const int* periodic, void* stream);
 
+/* ---- marker redistribution over the patches of a level ----------------- */
+/* One patch of a level: cell box and geometry (CartesianPatchGeometry). */
+typedef struct ibx_patch_box
+{
+    int ilower[3], iupper[3];
+    double x_lower[3], x_upper[3], dx[3];
+} ibx_patch_box;
+
+/* Which patch owns each marker (LDataManager::redistribute,
+ * src/IB/LDataManager.cpp:1351-1522, with the index rule of
+ * IndexUtilities::getCellIndex, ibtk/include/ibtk/private/
+ * IndexUtilities-inl.h:52-75, evaluated with every patch's geometry in FP64):
+ * owner[s] = the first patch in `patches` (a host array) whose cell box holds
+ * the marker's cell index, -1 for none; order = the markers grouped by owner
+ * (counting sort; patch p's markers are order[patch_offsets[p] ..
+ * patch_offsets[p+1]), the unowned ones follow, patch_offsets has
+ * n_patches + 2 entries and patch_offsets[n_patches + 1] = n_markers; the
+ * order within a patch is unspecified).  X, owner, order and patch_offsets
+ * are device arrays.  Uses stream-ordered scratch memory and synchronises
+ * the stream before returning. */
+int ibx_redistribute(int dim, const ibx_patch_box* patches, int n_patches, const double* X, int n_markers, int* owner,
+                     int* order, int* patch_offsets, void* stream);
+
 /* ---- Lagrangian forces before spreading -------------------------------- */
 /* IBStandardForceGen::computeLagrangianSpringForce
  * (src/IB/IBStandardForceGen.cpp:825-900) with the default linear spring
