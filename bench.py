@@ -63,6 +63,18 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(value, world, device):
+    """The largest value over the ranks (the job's time is its slowest
+    rank's); a no-op for one rank."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -287,10 +299,7 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     value = world * n / (ms * 1e-3)
 
     # ---- per-phase timing (same stream) for the roofline --------------------
@@ -376,10 +385,7 @@ def run_ours(args):
         step_e2e()
     barrier()
     ms_e2e = timed(step_e2e, args.steps)
-    if world > 1:
-        t = torch.tensor([ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(ms_e2e, world, dev)
     e2e = {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": X.size * 8 + F.size * 4,
            "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e}
 
@@ -515,10 +521,7 @@ def run_batched(args):
     ms = timed(B.replay, args.steps)
     barrier()
     clocks = sampler.stop()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     value = world * nm / (ms * 1e-3)
 
     reps = max(3, args.steps // 2)

@@ -6,8 +6,9 @@
  *
  * Every entry point is stream-ordered, reentrant and returns a status code
  * instead of aborting.  Pointers inside ibx_problem are DEVICE pointers
- * unless stated otherwise.  Nothing here allocates memory on the caller's
- * behalf except ibx_plan_create (see there).
+ * unless stated otherwise.  Only ibx_plan_create* allocate memory that
+ * outlives the call; ibx_spread / ibx_interpolate with several problems and
+ * ibx_redistribute use stream-ordered scratch freed before they return.
  *
  * Reference interfaces replaced (paths inside the IBAMR tree):
  *   LEI.h  = ibtk/include/ibtk/LEInteractor.h
