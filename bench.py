@@ -344,6 +344,7 @@ def run_ours(args):
     f_t2 = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
     plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED, tile_shape=plan.tile_shape[0])
     plan_e.set_tuning(*plan.tuning())
+    plan_e.visit_kernel = plan.visit_kernel
     plan_e.bin()
     plan_e.spread()
     fd = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
@@ -407,6 +408,7 @@ def run_ours(args):
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
             "tuning": None if tuned is None else {
                 "tile_shape": tuned["shape"], "tile_edges": list(plan_tile_edges),
+                "visit_kernel": tuned["visit_kernel"],
                 "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
                 "bin_spread_ms": tuned["ms"],
                 "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
@@ -602,7 +604,7 @@ def run_batched(args):
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
             "tuning": None if tuned is None else {
-                "tile_shape": tuned["shape"],
+                "tile_shape": tuned["shape"], "visit_kernel": tuned["visit_kernel"],
                 "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
                 "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * args.steps,

@@ -425,6 +425,20 @@ ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blo
 }
 
 int
+ibx_plan_set_visit_kernel(ibx_plan* plan, int form)
+{
+    if (!plan || form < 0 || form > 1) return IBX_E_ARG;
+    plan->D.visit_kernel = form;
+    return IBX_OK;
+}
+
+int
+ibx_plan_get_visit_kernel(const ibx_plan* plan)
+{
+    return plan ? plan->D.visit_kernel : -1;
+}
+
+int
 ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* dense_blocks_per_sm)
 {
     if (!plan) return IBX_E_ARG;

@@ -140,6 +140,7 @@ struct DevPlan
     int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
+    int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };

@@ -527,6 +527,110 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
         }
     }
 }
+// Visits of sparse-homed markers, second form: one lane per (visit,
+// component) work item, all components of the tile accumulated at once.
+// The lane keeps its visit's weights and accumulator offsets in registers
+// and runs the whole W^d footprint unrolled; points outside the tile are
+// masked by a negative offset and their atomics predicated off, so the warp
+// does not diverge.  Chosen by the autotuner when it is faster.
+constexpr int LANE_WARPS = 4; // tiles (warps) per CTA of this form
+
+__device__ __forceinline__ void
+acc2_always(float* hi, float* lo, float v)
+{
+    const float old = atomicAdd(hi, v);
+    const float s = old + v;
+    const float bp = s - old;
+    atomicAdd(lo, (old - (s - bp)) + (v - bp));
+}
+
+template <int DIM, int K, int SH>
+__global__ void __launch_bounds__(32 * LANE_WARPS, 4) spread_visits_lanes(const DevPlan D, int ncomp_max)
+{
+    constexpr int W = KT<K>::W;
+    using T = TileT<DIM, SH>;
+    using TL = TileLayout<DIM, SH>;
+    extern __shared__ float sm[]; // [LANE_WARPS][ncomp_max][hi, lo][SZ]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* acc = sm + warp * (2 * TL::SZ * ncomp_max);
+    for (int t = blockIdx.x * LANE_WARPS + warp; t < D.n_tiles; t += gridDim.x * LANE_WARPS)
+    {
+        const int vbeg = D.vcount[t];
+        const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
+        if (vend <= vbeg) continue;
+        const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
+        const PlanProb& P = D.probs[p];
+        int org[3];
+        tile_origin<DIM, SH>(P, t - P.tile0, org);
+        const int ncomp = P.ncomp;
+        for (int i = lane; i < ncomp * 2 * TL::SZ / 4; i += 32)
+            reinterpret_cast<float4*>(acc)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncwarp();
+        const float* Qf = static_cast<const float*>(P.Q);
+        const int nitems = (vend - vbeg) * ncomp;
+        for (int b0 = 0; b0 < nitems; b0 += 32)
+        {
+            const int it = b0 + lane;
+            if (it >= nitems) continue;
+            const int v = vbeg + it / ncomp;
+            const int c = it % ncomp;
+            const int g = D.visit_list[v];
+            const Rec R = D.rec[g];
+            float w[3][W];
+            int off[3][W];
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+            {
+                if (d >= DIM)
+                {
+#pragma unroll
+                    for (int i = 0; i < W; ++i)
+                    {
+                        w[d][i] = 1.f;
+                        off[d][i] = 0;
+                    }
+                    continue;
+                }
+                const bool stag = P.side && d == c;
+                const int b = stag ? R.bs[d] : R.bc[d];
+                weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
+                const int stride = d == 0 ? 1 : d == 1 ? TL::RS : TL::PS;
+#pragma unroll
+                for (int i = 0; i < W; ++i)
+                {
+                    const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                    off[d][i] = (l >= 0 && l < T::edge(d)) ? l * stride : -(1 << 20);
+                }
+            }
+            const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
+            float* hi = acc + c * 2 * TL::SZ;
+            float* lo = hi + TL::SZ;
+#pragma unroll
+            for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
+            {
+                const float wz = DIM == 3 ? w[2][i2] * V : V;
+                const int oz = DIM == 3 ? off[2][i2] : 0;
+#pragma unroll
+                for (int i1 = 0; i1 < W; ++i1)
+                {
+                    const float wyz = w[1][i1] * wz;
+                    const int oyz = off[1][i1] + oz;
+#pragma unroll
+                    for (int i0 = 0; i0 < W; ++i0)
+                    {
+                        const int idx = off[0][i0] + oyz;
+                        if (idx >= 0) acc2_always(hi + idx, lo + idx, w[0][i0] * wyz);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        for (int c = 0; c < ncomp; ++c)
+            tile_flush<DIM, SH>(P, org, c, acc + c * 2 * TL::SZ, acc + c * 2 * TL::SZ + TL::SZ, lane);
+        __syncwarp();
+    }
+}
+
 } // namespace
 
 namespace
@@ -548,6 +652,23 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
         spread_home_mixed<DIM, K, SH><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);
         note_launches(1);
         if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
+    }
+    if (D.visit_kernel == 1)
+    {
+        const size_t smem_l = sizeof(float) * 2 * TileLayout<DIM, SH>::SZ * max_ncomp * LANE_WARPS;
+        if (smem_l > 48 * 1024 &&
+            cudaFuncSetAttribute(spread_visits_lanes<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_l) != cudaSuccess)
+            return IBX_E_CUDA;
+        int per_sm_l = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_l, spread_visits_lanes<DIM, K, SH>, 32 * LANE_WARPS,
+                                                      smem_l);
+        if (per_sm_l < 1) per_sm_l = 1;
+        const unsigned need_l = (unsigned)((D.n_tiles + LANE_WARPS - 1) / LANE_WARPS);
+        const unsigned blocks_l = need_l < (unsigned)(per_sm_l * sms) ? need_l : (unsigned)(per_sm_l * sms);
+        spread_visits_lanes<DIM, K, SH><<<blocks_l, 32 * LANE_WARPS, smem_l, s>>>(D, max_ncomp);
+        note_launches(1);
+        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
     }
     const size_t smem_sparse = sizeof(float) * VisitSlots<DIM, W, SH>::words * SPARSE_WARPS;
     if (smem_sparse > 48 * 1024 &&

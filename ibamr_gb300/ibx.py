@@ -88,6 +88,8 @@ def lib():
             L.ibx_plan_n_tiles.argtypes = [ctypes.c_void_p]
             L.ibx_plan_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
             L.ibx_plan_get_tuning.argtypes = [ctypes.c_void_p, ip, ip, ip]
+            L.ibx_plan_set_visit_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.ibx_plan_get_visit_kernel.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -317,6 +319,17 @@ class Plan:
         e = (ctypes.c_int * 3)()
         sh = lib().ibx_plan_tile_shape(self.h, e)
         return sh, tuple(e)
+
+    @property
+    def visit_kernel(self):
+        """Form of the per-visit spread kernel (see ibx_plan_set_visit_kernel)."""
+        return lib().ibx_plan_get_visit_kernel(self.h)
+
+    @visit_kernel.setter
+    def visit_kernel(self, form):
+        rc = lib().ibx_plan_set_visit_kernel(self.h, int(form))
+        if rc:
+            raise IbxError(rc, "ibx_plan_set_visit_kernel")
 
     def tuning(self):
         """(item_units, dense_min, dense_blocks_per_sm)."""

@@ -1,6 +1,7 @@
 """Autotuner of the binned plan's spread.
 
-The spread of a plan has three knobs (``ibx_plan_set_tuning``): the number
+The spread of a plan has four knobs (``ibx_plan_set_tuning``,
+``ibx_plan_set_visit_kernel``): the form of the per-visit kernel, the number
 of home units per CTA of the dense-tile kernel (``item_units``, markers per
 block in effect), the home-marker count above which a tile is spread from
 its tile+halo region rather than through per-tile visits (``dense_min``,
@@ -25,6 +26,7 @@ DEFAULT_CANDIDATES = {
     "dense_min": (8, 16, 32, 64, 128, 256),
     "item_units": (32, 64, 128, 256),
     "dense_blocks_per_sm": (1, 2, 4),
+    "visit_kernel": (0, 1),
 }
 
 _cache = {}
@@ -55,6 +57,7 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
 
     if key is not None and key in _cache:
         plan.set_tuning(*_cache[key]["best"])
+        plan.visit_kernel = _cache[key]["visit_kernel"]
         return _cache[key]
     cand = dict(DEFAULT_CANDIDATES)
     if candidates:
@@ -82,7 +85,15 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     best, ms = min(table, key=lambda r: r[1])
     plan.set_tuning(*best)
     plan.bin()
-    out = {"best": best, "ms": ms, "table": table}
+    # the form of the per-visit kernel, at the best knobs
+    forms = []
+    for form in cand.get("visit_kernel", (0, 1)):
+        plan.visit_kernel = form
+        forms.append((form, _time(step, reps, stream)))
+    best_form, form_ms = min(forms, key=lambda r: r[1])
+    plan.visit_kernel = best_form
+    ms = min(ms, form_ms)
+    out = {"best": best, "ms": ms, "table": table, "visit_kernel": best_form, "visit_kernel_ms": forms}
     if key is not None:
         _cache[key] = out
     return out
@@ -100,7 +111,8 @@ def autotune_shape(make_plan, shapes=(0, 1), reps=3, candidates=None):
         if best is None or res["ms"] < best["ms"]:
             if best_plan is not None:
                 best_plan.close()
-            best_plan, best = plan, {"shape": sh, "ms": res["ms"], "best": res["best"]}
+            best_plan, best = plan, {"shape": sh, "ms": res["ms"], "best": res["best"],
+                                     "visit_kernel": res["visit_kernel"]}
         else:
             plan.close()
     best["per_shape"] = per

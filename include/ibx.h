@@ -264,6 +264,12 @@ int ibx_plan_n_tiles(const ibx_plan* plan);
  * next ibx_plan_bin. */
 int ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blocks_per_sm);
 int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* dense_blocks_per_sm);
+/* Form of the per-visit spread kernel (no reference counterpart; chosen by
+ * the autotuner): 0 = the in-tile points of 32 visits flattened over the
+ * lanes (default), 1 = one lane per (visit, component) with all components
+ * of the tile accumulated at once.  Same results up to FP32 rounding. */
+int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
+int ibx_plan_get_visit_kernel(const ibx_plan* plan);
 /* Bytes of device scratch the plan holds. */
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);

@@ -34,7 +34,7 @@ def seam_markers(rng, n, dim):
     return X.reshape(-1)
 
 
-def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, tile_shape=0):
+def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, tile_shape=0, visit_kernel=0):
     ncomp = dim if centering == ibx.SIDE else depth
     shape = list(N)[::-1]
     dx = [1.0 / v for v in N]
@@ -56,6 +56,7 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, til
     pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED, tile_shape=tile_shape)
     if dense_min is not None:
         ps.set_tuning(dense_min=dense_min)
+    ps.visit_kernel = visit_kernel
     ps.bin()
     ps.spread()
     pi.bin()
@@ -260,7 +261,7 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
     plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED)
     res = tuning.autotune(plan, reps=1, candidates={"dense_min": (0, 32, 1 << 30), "item_units": (32, 256),
                                                     "dense_blocks_per_sm": (1, 2)})
-    assert len(res["table"]) == 3 + 4
+    assert len(res["table"]) == 3 + 4 and res["visit_kernel"] in (0, 1)
     assert plan.tuning() == res["best"]
     assert res["ms"] == min(t for _, t in res["table"])
     for t in f_t:
@@ -379,3 +380,27 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim):
     assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
     assert plan.status() == ibx.OK
     plan.close()
+
+
+@pytest.mark.parametrize("tile_shape", [0, 1])
+@pytest.mark.parametrize("kernel", KERNEL_NAMES)
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("centering,depth", [(1, 1), (0, 2)])
+def test_visit_kernel_lane_form(ibx, oracle, kernel, dim, centering, depth, tile_shape):
+    """The lane-per-(visit, component) form of the per-visit kernel, every
+    marker spread through its visits, against the oracle."""
+    rng = np.random.default_rng(71 + dim + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
+    N = [29, 22, 18][:dim] if dim == 3 else [45, 38]
+    n = 2500
+    X = seam_markers(rng, n, dim)
+    ncomp = dim if centering == 1 else depth
+    F = rng.standard_normal(n * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
+    f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=1 << 30,
+                            tile_shape=tile_shape, visit_kernel=1)
+    assert ps.visit_kernel == 1
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(U, U_ref) <= MIXED_TOL
+    ps.close()
+    pi.close()
