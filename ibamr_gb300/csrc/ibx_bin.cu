@@ -123,24 +123,17 @@ base_r_fixed(long long Xf, long long xlo_f, long long inv_f, int F, int dshift, 
     return true;
 }
 
-// Warp-aggregated counter increment: lanes with equal keys share one atomic;
-// returns the old value plus the lane's rank among them.
-__device__ __forceinline__ int
-agg_add(int* counters, int key, bool valid)
+// Warp-aggregated counter increment (no result is read back, so the add
+// compiles to a reduction): one atomic per group of lanes with equal keys.
+__device__ __forceinline__ void
+agg_count(int* counters, int key, bool valid)
 {
     const unsigned act = __ballot_sync(__activemask(), valid);
-    int res = 0;
     if (valid)
     {
         const unsigned grp = __match_any_sync(act, key);
-        const int lane = threadIdx.x & 31;
-        const int leader = __ffs(grp) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(&counters[key], __popc(grp));
-        base = __shfl_sync(grp, base, leader);
-        res = base + __popc(grp & ((1u << lane) - 1));
+        if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&counters[key], __popc(grp));
     }
-    return res;
 }
 
 // Distinct tiles (along one dim) holding the cells (b+i) mod N, i in [0, span).
@@ -173,8 +166,8 @@ visit_tiles(const PlanProb& P, const Rec& R, int (*tl)[4], int* nt)
             tl[d][0] = 0;
             continue;
         }
-        const int lo = P.side ? min((int)R.bc[d], (int)R.bs[d]) : R.bc[d];
-        const int hi = (P.side ? max((int)R.bc[d], (int)R.bs[d]) : R.bc[d]) + W - 1;
+        const int lo = R.bc(d);
+        const int hi = R.bc(d) + (P.side ? R.stagger(d) : 0) + W - 1;
         nt[d] = tiles_1d(lo, hi - lo + 1, P.N[d], TileT<DIM, SH>::edge(d), tl[d]);
         total *= nt[d];
     }
@@ -191,20 +184,12 @@ visit_tile_id(const PlanProb& P, int (*tl)[4], const int* nt, int k)
     return P.tile0 + tl[0][c0] + P.ntile[0] * (tl[1][c1] + P.ntile[1] * tl[2][c2]);
 }
 
-// The stencil bases of a record packed into one 64-bit key: markers with
-// equal keys share the stencil of every component.
-template <int DIM>
+// The stencil bases of a record as one 64-bit key: markers with equal keys
+// share the stencil of every component.
 __device__ __forceinline__ unsigned long long
 base_key(const Rec& R)
 {
-    unsigned long long k = 0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d)
-    {
-        k |= (unsigned long long)(unsigned short)R.bc[d] << (16 * d);
-        k |= (unsigned long long)((R.bs[d] - R.bc[d]) & 1) << (48 + d);
-    }
-    return k;
+    return R.key;
 }
 
 // Lanes of the active set that share both the tile and the stencil key.
@@ -232,12 +217,12 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
     {
         const long long s = g - P.marker0;
         bool finite = true;
+        unsigned long long rkey = 0;
 #pragma unroll
         for (int d = 0; d < 3; ++d)
         {
             if (d >= DIM)
             {
-                R.bc[d] = R.bs[d] = 0;
                 R.rc[d] = R.rs[d] = 0.f;
                 continue;
             }
@@ -258,12 +243,14 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
             const int shift = (bc >= 0 ? bc / N : -((-bc + N - 1) / N)) * N;
             bc -= shift;
             bs -= shift;
-            R.bc[d] = (short)bc;
-            R.bs[d] = (short)bs;
+            rkey |= (unsigned long long)(unsigned short)bc << (16 * d);
+            rkey |= (unsigned long long)(bs - bc == 1) << (48 + d);
+            finite = finite && (bs - bc == 0 || bs - bc == 1);
             R.rc[d] = rc;
             R.rs[d] = rs;
             home[d] = wrap_cell(bc + (W - 1) / 2, N) / TileT<DIM, SH>::edge(d);
         }
+        R.key = rkey;
         if (!finite)
         {
             // Reported through the plan's status word; the marker is skipped.
@@ -279,7 +266,7 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
         D.rec[g] = R;
         ht = P.tile0 + home[0] + P.ntile[0] * (home[1] + (DIM == 3 ? P.ntile[1] * home[2] : 0));
         D.home_tile[g] = ht;
-        key = base_key<DIM>(R);
+        key = base_key(R);
     }
     const unsigned act = __ballot_sync(0xffffffffu, valid);
     bool lead = false;
@@ -288,8 +275,8 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
         const unsigned grp = unit_group(act, ht, key);
         lead = (threadIdx.x & 31) == __ffs(grp) - 1;
     }
-    agg_add(D.hcount, ht, valid);
-    agg_add(D.hucount, ht, lead);
+    agg_count(D.hcount, ht, valid);
+    agg_count(D.hucount, ht, lead);
 }
 
 // Places a unit group: its leader reserves a contiguous range of the list
@@ -334,7 +321,7 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
     if (valid)
     {
         R = D.rec[g];
-        key = base_key<DIM>(R);
+        key = base_key(R);
     }
     {
         const unsigned act = __ballot_sync(0xffffffffu, valid);
@@ -358,8 +345,8 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
             const unsigned grp = unit_group(act, t, key);
             lead = (threadIdx.x & 31) == __ffs(grp) - 1;
         }
-        agg_add(D.vcount, t, v);
-        agg_add(D.ucount, t, lead);
+        agg_count(D.vcount, t, v);
+        agg_count(D.ucount, t, lead);
     }
 }
 
@@ -379,7 +366,7 @@ __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
     {
         const Rec R = D.rec[g];
         nvis = visit_tiles<DIM, K, SH>(P, R, tl, nt);
-        key = base_key<DIM>(R);
+        key = base_key(R);
     }
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_home_mixed(const DevPla
                 continue;
             }
             const bool stag = P.side && d == c;
-            b[d] = stag ? R.bs[d] : R.bc[d];
+            b[d] = stag ? R.bs(d) : R.bc(d);
             weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
         }
         const float* q = static_cast<const float*>(P.qi[c]);

@@ -383,8 +383,8 @@ ibx_plan_get_bins(const ibx_plan* plan, int* base_c, int* base_s, int* home_tile
         for (long long g = 0; g < nm; ++g)
             for (int d = 0; d < 3; ++d)
             {
-                if (base_c) base_c[3 * g + d] = rec[g].bc[d];
-                if (base_s) base_s[3 * g + d] = rec[g].bs[d];
+                if (base_c) base_c[3 * g + d] = rec[g].bc(d);
+                if (base_s) base_s[3 * g + d] = rec[g].bs(d);
             }
     }
     if (home_tile && nm && cudaMemcpy(home_tile, D.home_tile, sizeof(int) * nm, cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -51,19 +51,27 @@ tile_edges(int dim, int shape, int* e)
     e[2] = dim == 3 ? 8 : 1;
 }
 
-// Per-marker stencil record (48 bytes).  For every dimension: the stencil
-// base (relative to the box's lower index, shifted by a multiple of N into
-// [0, N) for the cell-centred one) of the cell-centred and of the staggered
-// (side-normal) position, and r_first = t - (base + 1/2), the distance in
-// cells of the marker from the first stencil point, computed exactly and
-// rounded once to FP32.
+// Per-marker stencil record (32 bytes: one DRAM sector).  For every
+// dimension: the stencil base (relative to the box's lower index, shifted by
+// a multiple of N into [0, N) for the cell-centred one) of the cell-centred
+// and of the staggered (side-normal) position, and r_first = t - (base +
+// 1/2), the distance in cells of the marker from the first stencil point,
+// computed exactly and rounded once to FP32.  The staggered position is half
+// a cell above the cell-centred one, so its base is the cell-centred base or
+// the next cell: the bases pack into one word, 16 bits of cell-centred base
+// per dimension and one bit per dimension for the staggered step.  Markers
+// with equal words share the stencils of every component.
 struct __align__(16) Rec
 {
     float rc[3];
     float rs[3];
-    short bc[3];
-    short bs[3];
+    unsigned long long key;
+
+    __host__ __device__ __forceinline__ int bc(int d) const { return (short)(unsigned short)(key >> (16 * d)); }
+    __host__ __device__ __forceinline__ int bs(int d) const { return bc(d) + (int)((key >> (48 + d)) & 1u); }
+    __host__ __device__ __forceinline__ int stagger(int d) const { return (int)((key >> (48 + d)) & 1u); }
 };
+static_assert(sizeof(Rec) == 32, "one record per 32-byte sector");
 
 // Exact fixed-point description of t = (X - x_lower)/dx for one dimension
 // (see ibx_bin.cu): Xf = floor(X*2^sx), D = Xf - xlo_f, T = mulhi(D, inv_f),

@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
 #pragma unroll
                     for (int d = 0; d < DIM; ++d)
                     {
-                        const int st = (P.side && d == c) ? min(max(R0.bs[d] - R0.bc[d], 0), 1) : 0; // 0 or 1
-                        s0[d] = wrap_cell(R0.bc[d] + (W - 1) / 2, P.N[d]) - org[d] + st;
+                        const int st = (P.side && d == c) ? R0.stagger(d) : 0; // 0 or 1
+                        s0[d] = wrap_cell(R0.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + st;
                     }
                 }
                 // Markers of the unit, software-pipelined: the next marker's
@@ -271,8 +271,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                     for (int d = 0; d < DIM; ++d)
                     {
                         const bool st = P.side && d == c;
-                        s0[d] = wrap_cell(R.bc[d] + (W - 1) / 2, P.N[d]) - org[d] +
-                                (st ? min(max(R.bs[d] - R.bc[d], 0), 1) : 0);
+                        s0[d] = wrap_cell(R.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + (st ? R.stagger(d) : 0);
                         weights_f32<K>(st ? R.rs[d] : R.rc[d], w[d]);
                     }
                     const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
@@ -438,7 +437,7 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
                     for (int d = 0; d < DIM; ++d)
                     {
                         const bool stag = P.side && d == c;
-                        const int b = stag ? R.bs[d] : R.bc[d];
+                        const int b = stag ? R.bs(d) : R.bc(d);
                         weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
                         const int stride = d == 0 ? 1 : d == 1 ? TL::RS : TL::PS;
                         int n = 0;
@@ -592,7 +591,7 @@ __global__ void __launch_bounds__(32 * LANE_WARPS, 4) spread_visits_lanes(const 
                     continue;
                 }
                 const bool stag = P.side && d == c;
-                const int b = stag ? R.bs[d] : R.bc[d];
+                const int b = stag ? R.bs(d) : R.bc(d);
                 weights_f32<K>(stag ? R.rs[d] : R.rc[d], w[d]);
                 const int stride = d == 0 ? 1 : d == 1 ? TL::RS : TL::PS;
 #pragma unroll

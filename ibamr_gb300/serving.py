@@ -38,7 +38,7 @@ def plan_bytes_estimate(dim, N, n_markers):
         per *= min(nt, 2 + (n % E != 0))
     visit_cap = n_markers * per
     b = 0
-    b += 2 * 48 * n_markers                     # records (marker order, home order)
+    b += 2 * 32 * n_markers                     # records (marker order, home order)
     b += 3 * 4 * n_markers + 8 * n_markers      # home tile, home list, home units
     b += visit_cap * (4 + 8)                    # visit list, visit units
     b += 4 * (9 * tiles + 5)                    # counters

@@ -50,8 +50,10 @@ def _time(fn, reps, stream):
 def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     """Measure every candidate setting of ``plan`` and keep the fastest.
 
-    Returns {"best": (item_units, dense_min, dense_blocks_per_sm), "ms": t,
-    "table": [((...), ms), ...]}.  With ``key`` the result is cached for
+    Returns {"best": (item_units, dense_min, dense_blocks_per_sm),
+    "table": [((...), ms), ...], "visit_kernel": form, "visit_kernel_ms":
+    [(form, ms), ...], "ms": t}, t being the time of the applied setting
+    (best knobs and best form).  With ``key`` the result is cached for
     this process and later calls with the same key only apply it."""
     import torch
 
@@ -82,7 +84,7 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
         plan.set_tuning(iu, best_dm, bps)
         plan.bin()
         table.append((plan.tuning(), _time(step, reps, stream)))
-    best, ms = min(table, key=lambda r: r[1])
+    best = min(table, key=lambda r: r[1])[0]
     plan.set_tuning(*best)
     plan.bin()
     # the form of the per-visit kernel, at the best knobs
@@ -90,9 +92,8 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     for form in cand.get("visit_kernel", (0, 1)):
         plan.visit_kernel = form
         forms.append((form, _time(step, reps, stream)))
-    best_form, form_ms = min(forms, key=lambda r: r[1])
+    best_form, ms = min(forms, key=lambda r: r[1])
     plan.visit_kernel = best_form
-    ms = min(ms, form_ms)
     out = {"best": best, "ms": ms, "table": table, "visit_kernel": best_form, "visit_kernel_ms": forms}
     if key is not None:
         _cache[key] = out

@@ -263,7 +263,8 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
                                                     "dense_blocks_per_sm": (1, 2)})
     assert len(res["table"]) == 3 + 4 and res["visit_kernel"] in (0, 1)
     assert plan.tuning() == res["best"]
-    assert res["ms"] == min(t for _, t in res["table"])
+    assert res["best"] == min(res["table"], key=lambda r: r[1])[0]
+    assert res["ms"] == min(t for _, t in res["visit_kernel_ms"])
     for t in f_t:
         t.zero_()
     plan.bin()
