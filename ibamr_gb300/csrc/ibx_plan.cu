@@ -130,6 +130,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.n_item_cap = (int)z.item_cap;
     D.item_units = ITEM_UNITS;
     D.dense_min = DENSE_MIN;
+    D.dense_interp = 1;
     D.tile_shape = z.tile_shape;
     D.dense_blocks_per_sm = 2;
     D.status = reinterpret_cast<int*>(b + c.o_status);
@@ -149,8 +150,10 @@ struct ibx_plan
     size_t dbytes;
     int* scan_tmp;
     // ibx_plan_step: interpolation forks onto `side` after the binning
+    // (step_mode 1) or follows the spread on the caller's stream (0)
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_join;
+    int step_mode;
 };
 
 extern "C" {
@@ -259,6 +262,8 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         }
         P.vec4 = P.N[0] % 4 == 0;
         for (int c = 0; c < ncomp; ++c) P.vec4 = P.vec4 && (reinterpret_cast<unsigned long long>(P.q[c]) & 15) == 0;
+        P.vec4i = P.N[0] % 4 == 0;
+        for (int c = 0; c < ncomp; ++c) P.vec4i = P.vec4i && (reinterpret_cast<unsigned long long>(P.qi[c]) & 15) == 0;
         P.tile0 = toffs[p];
         P.marker0 = moffs[p];
         if ((long long)toffs[p] + ntiles > 0x3fffffffLL) return IBX_E_TOO_LARGE;
@@ -308,6 +313,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         return IBX_E_CUDA;
     }
     plan->scan_tmp = c.scan_tmp;
+    plan->step_mode = 1;
     if (cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess)
@@ -341,6 +347,11 @@ ibx_plan_step(ibx_plan* plan, void* stream)
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s);
     if (rc) return rc;
+    if (plan->step_mode == 0)
+    {
+        rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
+        return rc ? rc : launch_interp(plan->dim, plan->kernel, plan->D, s);
+    }
     // spread (stream) and interpolation (side) read the same bins and write
     // different arrays: they overlap on the device
     if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
@@ -427,7 +438,7 @@ ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blo
 int
 ibx_plan_set_visit_kernel(ibx_plan* plan, int form)
 {
-    if (!plan || form < 0 || form > 1) return IBX_E_ARG;
+    if (!plan || form < 0 || form > 2) return IBX_E_ARG;
     plan->D.visit_kernel = form;
     return IBX_OK;
 }
@@ -436,6 +447,34 @@ int
 ibx_plan_get_visit_kernel(const ibx_plan* plan)
 {
     return plan ? plan->D.visit_kernel : -1;
+}
+
+int
+ibx_plan_set_step_mode(ibx_plan* plan, int mode)
+{
+    if (!plan || mode < 0 || mode > 1) return IBX_E_ARG;
+    plan->step_mode = mode;
+    return IBX_OK;
+}
+
+int
+ibx_plan_get_step_mode(const ibx_plan* plan)
+{
+    return plan ? plan->step_mode : -1;
+}
+
+int
+ibx_plan_set_interp_kernel(ibx_plan* plan, int form)
+{
+    if (!plan || form < 0 || form > 1) return IBX_E_ARG;
+    plan->D.dense_interp = form;
+    return IBX_OK;
+}
+
+int
+ibx_plan_get_interp_kernel(const ibx_plan* plan)
+{
+    return plan ? plan->D.dense_interp : -1;
 }
 
 int

@@ -99,6 +99,7 @@ struct PlanProb
     FixedDim fx[3];
     float inv_vol;     // 1/(dx0*dx1[*dx2]) rounded to FP32
     int vec4;          // N[0] % 4 == 0 and every spread target 16-byte aligned
+    int vec4i;         // N[0] % 4 == 0 and every interpolation source 16-byte aligned
     const double* X;
     void* Q;           // spread source
     void* q[3];        // spread target, one array per component (side axis or cell depth)
@@ -149,6 +150,7 @@ struct DevPlan
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
     int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component)
+    int dense_interp; // 1: dense-homed markers interpolated per home unit
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
@@ -209,6 +211,17 @@ wrap_cell(int c, int N)
     while (c >= N) c -= N;
     while (c < 0) c += N;
     return c;
+}
+
+// First cell of local tile lt of a problem.
+template <int DIM, int SH>
+__device__ __forceinline__ void
+tile_origin(const PlanProb& P, int lt, int* org)
+{
+    using T = TileT<DIM, SH>;
+    org[0] = (lt % P.ntile[0]) * T::E0;
+    org[1] = ((lt / P.ntile[0]) % P.ntile[1]) * T::E1;
+    org[2] = DIM == 3 ? (lt / (P.ntile[0] * P.ntile[1])) * T::E2 : 0;
 }
 
 // ---- FP32 weights (mixed form) --------------------------------------------

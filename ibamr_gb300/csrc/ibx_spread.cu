@@ -67,16 +67,6 @@ struct Region
     static constexpr int CSTR = pad_to(2 * PAD, 32, 8);  // words per component (hi, lo)
 };
 
-template <int DIM, int SH>
-__device__ __forceinline__ void
-tile_origin(const PlanProb& P, int lt, int* org)
-{
-    using T = TileT<DIM, SH>;
-    org[0] = (lt % P.ntile[0]) * T::E0;
-    org[1] = ((lt / P.ntile[0]) % P.ntile[1]) * T::E1;
-    org[2] = DIM == 3 ? (lt / (P.ntile[0] * P.ntile[1])) * T::E2 : 0;
-}
-
 // q + hi + lo rounded to FP32 without FP64 arithmetic (GB300 runs FP64 at a
 // small fraction of the FP32 rate): s + e = q + hi exactly (Knuth TwoSum),
 // then s + (e + lo); the result is within one FP32 ulp of the exact sum.
@@ -630,6 +620,180 @@ __global__ void __launch_bounds__(32 * LANE_WARPS, 4) spread_visits_lanes(const 
     }
 }
 
+
+// Visits of sparse-homed markers, third form: the tile gathered rather than
+// scattered.  A visit's contribution to one component of a tile is the outer
+// product of its separable weights restricted to the tile, w0(x) w1(y)
+// w2(z) Q/vol, so the tile's sum over its visits is a small contraction:
+// lane l owns CPL values of the tile (NR rows of SX consecutive x) in
+// registers, and for every visit adds a(row) * b(x) with a(row) = w1(y) *
+// (w2(z) * Q/vol) and b(x) = w0(x), reading the visit's tile-restricted
+// weight vectors (zero outside its stencil) from shared memory.  No atomics:
+// every lane updates only its own values, all lanes run every visit, and the
+// warp then adds the tile to the grid with coalesced read-modify-writes.
+// Sums over batches of 32 visits are folded into a double-FP32 pair with
+// Knuth TwoSum, so the error bound is that of 32-term FP32 sums.
+template <int DIM, int SH>
+struct GatherLayout
+{
+    using T = TileT<DIM, SH>;
+    static constexpr int CPL = T::PTS / 32;                  // values per lane
+    static constexpr int SX = CPL < T::E0 ? CPL : T::E0;     // consecutive x per lane row
+    static constexpr int NR = CPL / SX;                      // rows per lane
+    static constexpr int VW = T::E0 + T::E1 + T::E2;         // weight vector words of a visit
+    static constexpr int SS = ((VW + 3) / 8) * 8 + 4;        // slot stride: = 4 mod 8 (float4-aligned)
+    static_assert(CPL * 32 == T::PTS && SX % 4 == 0 && NR * SX == CPL, "lane layout covers the tile");
+};
+
+constexpr int GATHER_WARPS = 8; // tiles (warps) per CTA of the gather form
+
+// CTAs per SM the register budget is cut for: 3 x (256 threads) with 16
+// values per lane, 1 with 32 (3D tiles of 16 x 8 x 8).
+template <int DIM, int SH>
+struct GatherOccupancy
+{
+    static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 3;
+};
+
+template <int DIM, int K, int SH>
+__global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::value)
+    spread_visits_gather(const DevPlan D)
+{
+    constexpr int W = KT<K>::W;
+    using T = TileT<DIM, SH>;
+    using GL = GatherLayout<DIM, SH>;
+    constexpr int CPL = GL::CPL, SX = GL::SX, NR = GL::NR, SS = GL::SS;
+    extern __shared__ float sm[]; // [GATHER_WARPS][32][SS]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* slots = sm + warp * 32 * SS;
+    float* mine = slots + lane * SS;
+    // this lane's values: rows r0 .. r0 + NR - 1 (row = y + E1 * z), x in [xs, xs + SX)
+    const int first = lane * CPL;
+    const int r0 = first / T::E0;
+    const int xs = first % T::E0;
+    for (int t = blockIdx.x * GATHER_WARPS + warp; t < D.n_tiles; t += gridDim.x * GATHER_WARPS)
+    {
+        const int vbeg = D.vcount[t];
+        const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
+        if (vend <= vbeg) continue;
+        const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
+        const PlanProb& P = D.probs[p];
+        int org[3];
+        tile_origin<DIM, SH>(P, t - P.tile0, org);
+        const float* Qf = static_cast<const float*>(P.Q);
+        for (int c = 0; c < P.ncomp; ++c)
+        {
+            float hi[CPL], lo[CPL];
+#pragma unroll
+            for (int i = 0; i < CPL; ++i) hi[i] = lo[i] = 0.f;
+            for (int b0 = vbeg; b0 < vend; b0 += 32)
+            {
+                const int nb = min(32, vend - b0);
+                // -- this lane's visit: its weight vectors restricted to the tile
+#pragma unroll
+                for (int i = 0; i < SS / 4; ++i) reinterpret_cast<float4*>(mine)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (lane < nb)
+                {
+                    const int g = D.visit_list[b0 + lane];
+                    const Rec R = D.rec[g];
+                    const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                    {
+                        const bool stag = P.side && d == c;
+                        const int b = stag ? R.bs(d) : R.bc(d);
+                        float w[W];
+                        weights_f32<K>(stag ? R.rs[d] : R.rc[d], w);
+                        const int off = d == 0 ? 0 : d == 1 ? T::E0 : T::E0 + T::E1;
+#pragma unroll
+                        for (int i = 0; i < W; ++i)
+                        {
+                            const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                            // Q/vol rides on the last dimension's weights
+                            if (l >= 0 && l < T::edge(d)) mine[off + l] += d == DIM - 1 ? w[i] * V : w[i];
+                        }
+                    }
+                }
+                __syncwarp();
+                // -- the batch's contraction into this lane's values
+                float acc[CPL];
+#pragma unroll
+                for (int i = 0; i < CPL; ++i) acc[i] = 0.f;
+                for (int m = 0; m < nb; ++m)
+                {
+                    const float* sv = slots + m * SS;
+                    float bx[SX];
+#pragma unroll
+                    for (int i = 0; i < SX / 4; ++i)
+                    {
+                        const float4 q4 = *reinterpret_cast<const float4*>(sv + xs + 4 * i);
+                        bx[4 * i] = q4.x;
+                        bx[4 * i + 1] = q4.y;
+                        bx[4 * i + 2] = q4.z;
+                        bx[4 * i + 3] = q4.w;
+                    }
+#pragma unroll
+                    for (int k = 0; k < NR; ++k)
+                    {
+                        const int r = r0 + k;
+                        const float a = DIM == 3 ? sv[T::E0 + r % T::E1] * sv[T::E0 + T::E1 + r / T::E1]
+                                                 : sv[T::E0 + r];
+#pragma unroll
+                        for (int i = 0; i < SX; ++i) acc[k * SX + i] = fmaf(bx[i], a, acc[k * SX + i]);
+                    }
+                }
+                // -- fold the batch sums into the double-FP32 pair
+#pragma unroll
+                for (int i = 0; i < CPL; ++i)
+                {
+                    const float s = hi[i] + acc[i];
+                    const float bp = s - hi[i];
+                    lo[i] += (hi[i] - (s - bp)) + (acc[i] - bp);
+                    hi[i] = s;
+                }
+                __syncwarp();
+            }
+            // -- q += hi + lo for this lane's values
+            float* q = static_cast<float*>(P.q[c]);
+#pragma unroll
+            for (int k = 0; k < NR; ++k)
+            {
+                const int r = r0 + k;
+                const int y = org[1] + r % T::E1;
+                const int z = DIM == 3 ? org[2] + r / T::E1 : 0;
+                if (y >= P.N[1] || (DIM == 3 && z >= P.N[2])) continue;
+                const int x0 = org[0] + xs;
+                const long long o = x0 + (long long)P.N[0] * (y + (long long)P.N[1] * z);
+                const bool vec = P.vec4 && x0 + SX <= P.N[0];
+#pragma unroll
+                for (int i = 0; i < SX; i += 4)
+                {
+                    const float* h = hi + k * SX + i;
+                    const float* l = lo + k * SX + i;
+                    if (h[0] == 0.f && h[1] == 0.f && h[2] == 0.f && h[3] == 0.f && l[0] == 0.f && l[1] == 0.f &&
+                        l[2] == 0.f && l[3] == 0.f)
+                        continue;
+                    if (vec)
+                    {
+                        float4 v = *reinterpret_cast<float4*>(q + o + i);
+                        v.x = merge3(v.x, h[0], l[0]);
+                        v.y = merge3(v.y, h[1], l[1]);
+                        v.z = merge3(v.z, h[2], l[2]);
+                        v.w = merge3(v.w, h[3], l[3]);
+                        *reinterpret_cast<float4*>(q + o + i) = v;
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (x0 + i + e < P.N[0] && (h[e] != 0.f || l[e] != 0.f))
+                                q[o + i + e] = merge3(q[o + i + e], h[e], l[e]);
+                    }
+                }
+            }
+        }
+    }
+}
 } // namespace
 
 namespace
@@ -651,6 +815,24 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
         spread_home_mixed<DIM, K, SH><<<dense_blocks, UNIT_THREADS, smem, s>>>(D);
         note_launches(1);
         if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
+    }
+    if (D.visit_kernel == 2)
+    {
+        using GL = GatherLayout<DIM, SH>;
+        const size_t smem_g = sizeof(float) * 32 * GL::SS * GATHER_WARPS;
+        if (smem_g > 48 * 1024 &&
+            cudaFuncSetAttribute(spread_visits_gather<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_g) != cudaSuccess)
+            return IBX_E_CUDA;
+        int per_sm_g = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_g, spread_visits_gather<DIM, K, SH>,
+                                                      32 * GATHER_WARPS, smem_g);
+        if (per_sm_g < 1) per_sm_g = 1;
+        const unsigned need_g = (unsigned)((D.n_tiles + GATHER_WARPS - 1) / GATHER_WARPS);
+        const unsigned blocks_g = need_g < (unsigned)(per_sm_g * sms) ? need_g : (unsigned)(per_sm_g * sms);
+        spread_visits_gather<DIM, K, SH><<<blocks_g, 32 * GATHER_WARPS, smem_g, s>>>(D);
+        note_launches(1);
+        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
     }
     if (D.visit_kernel == 1)
     {

@@ -90,6 +90,10 @@ def lib():
             L.ibx_plan_get_tuning.argtypes = [ctypes.c_void_p, ip, ip, ip]
             L.ibx_plan_set_visit_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.ibx_plan_get_visit_kernel.argtypes = [ctypes.c_void_p]
+            L.ibx_plan_set_interp_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.ibx_plan_get_interp_kernel.argtypes = [ctypes.c_void_p]
+            L.ibx_plan_set_step_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.ibx_plan_get_step_mode.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -276,6 +280,13 @@ class Plan:
             raise IbxError(rc, "ibx_plan_create")
         self.h = h
 
+    @property
+    def separate_interp(self):
+        """True when the plan interpolates into its own targets (interp_problems
+        given); otherwise interpolation reads the spread targets and writes
+        the spread sources."""
+        return self._problems[1] is not None
+
     def bin(self, stream=None):
         rc = lib().ibx_plan_bin(self.h, _stream_handle(stream))
         if rc:
@@ -330,6 +341,28 @@ class Plan:
         rc = lib().ibx_plan_set_visit_kernel(self.h, int(form))
         if rc:
             raise IbxError(rc, "ibx_plan_set_visit_kernel")
+
+    @property
+    def interp_kernel(self):
+        """Form of the interpolation (see ibx_plan_set_interp_kernel)."""
+        return lib().ibx_plan_get_interp_kernel(self.h)
+
+    @interp_kernel.setter
+    def interp_kernel(self, form):
+        rc = lib().ibx_plan_set_interp_kernel(self.h, int(form))
+        if rc:
+            raise IbxError(rc, "ibx_plan_set_interp_kernel")
+
+    @property
+    def step_mode(self):
+        """Order of spread and interpolation in step() (see ibx_plan_set_step_mode)."""
+        return lib().ibx_plan_get_step_mode(self.h)
+
+    @step_mode.setter
+    def step_mode(self, mode):
+        rc = lib().ibx_plan_set_step_mode(self.h, int(mode))
+        if rc:
+            raise IbxError(rc, "ibx_plan_set_step_mode")
 
     def tuning(self):
         """(item_units, dense_min, dense_blocks_per_sm)."""

@@ -1,15 +1,25 @@
-"""Autotuner of the binned plan's spread.
+"""Autotuner of the binned plan.
 
-The spread of a plan has four knobs (``ibx_plan_set_tuning``,
-``ibx_plan_set_visit_kernel``): the form of the per-visit kernel, the number
-of home units per CTA of the dense-tile kernel (``item_units``, markers per
-block in effect), the home-marker count above which a tile is spread from
-its tile+halo region rather than through per-tile visits (``dense_min``,
-which decides the split between the two kernels), and the CTAs per SM of
-the dense-tile kernel.  The best setting depends on the marker distribution
-(clustered fibres favour regions, scattered markers favour visits), so it
-is measured: every candidate runs ``bin`` + ``spread`` on the plan's own
-data and the fastest is kept.
+A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
+``ibx_plan_set_interp_kernel``, ``ibx_plan_set_step_mode``):
+
+* ``dense_min``: the home-marker count above which a tile is spread from its
+  tile+halo region rather than through per-tile visits (the split between
+  the two spread kernels);
+* ``visit_kernel``: the form of the per-visit spread kernel (points
+  flattened over lanes, lane per visit, or the tile gathered in registers);
+* ``item_units`` and ``dense_blocks_per_sm``: home units per CTA work item
+  and CTAs per SM of the dense-tile kernel;
+* ``interp_kernel``: dense-homed markers interpolated per home unit, or all
+  markers in chunks;
+* ``step_mode``: spread and interpolation concurrent or one after the other
+  in ``step``.
+
+The best setting depends on the marker distribution (clustered fibres favour
+regions, scattered markers favour visits), so it is measured: every
+candidate runs ``bin`` + ``spread`` on the plan's own data (the whole
+``step``, interpolation included, when the plan has its own interpolation
+targets) and the fastest is kept.
 
 The tile shape is a property of a plan, chosen when it is created
 (``autotune_shape`` builds one plan per shape, tunes each, and keeps the
@@ -26,7 +36,9 @@ DEFAULT_CANDIDATES = {
     "dense_min": (8, 16, 32, 64, 128, 256),
     "item_units": (32, 64, 128, 256),
     "dense_blocks_per_sm": (1, 2, 4),
-    "visit_kernel": (0, 1),
+    "visit_kernel": (0, 1, 2),
+    "interp_kernel": (1, 0),
+    "step_mode": (1, 0),
 }
 
 _cache = {}
@@ -48,18 +60,35 @@ def _time(fn, reps, stream):
 
 
 def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
-    """Measure every candidate setting of ``plan`` and keep the fastest.
+    """Measure candidate settings of ``plan`` and keep the fastest.
 
-    Returns {"best": (item_units, dense_min, dense_blocks_per_sm),
-    "table": [((...), ms), ...], "visit_kernel": form, "visit_kernel_ms":
-    [(form, ms), ...], "ms": t}, t being the time of the applied setting
-    (best knobs and best form).  With ``key`` the result is cached for
-    this process and later calls with the same key only apply it."""
+    The search runs in three stages, each at the best setting so far: the
+    split between the two spread kernels (``dense_min``) jointly with the
+    per-visit kernel form; the dense-kernel knobs (``item_units``,
+    ``dense_blocks_per_sm``); for plans with their own interpolation targets,
+    the interpolation form jointly with the step mode (concurrent or serial
+    spread and interpolation).  Returns {"best": (item_units, dense_min,
+    dense_blocks_per_sm), "visit_kernel": form, "interp_kernel": form or
+    None, "step_mode": mode or None, "ms": t, "table": [((item_units,
+    dense_min, dense_blocks_per_sm, visit_kernel, interp_kernel, step_mode),
+    ms), ...]}, t being the time of the applied setting.  With ``key`` the
+    result is cached for this process and later calls with the same key only
+    apply it."""
     import torch
 
+    full = include_bin and getattr(plan, "separate_interp", False)
+
+    def apply(cfg):
+        iu, dm, bps, vk, ik, sm = cfg
+        plan.set_tuning(iu, dm, bps)
+        plan.visit_kernel = vk
+        if full:
+            plan.interp_kernel = ik
+            plan.step_mode = sm
+        plan.bin()
+
     if key is not None and key in _cache:
-        plan.set_tuning(*_cache[key]["best"])
-        plan.visit_kernel = _cache[key]["visit_kernel"]
+        apply(_cache[key]["config"])
         return _cache[key]
     cand = dict(DEFAULT_CANDIDATES)
     if candidates:
@@ -67,34 +96,37 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     stream = torch.cuda.current_stream()
 
     def step():
+        if full:
+            plan.step()
+            return
         if include_bin:
             plan.bin()
         plan.spread()
 
     table = []
-    # dense_min changes the binning: search it first with the other knobs
-    # at their defaults, then the dense-kernel knobs at the best split.
+
+    def measure(cfg):
+        apply(cfg)
+        table.append((cfg, _time(step, reps, stream)))
+
+    def best_cfg():
+        return min(table, key=lambda r: r[1])
+
     iu0, dm0, bps0 = plan.tuning()
-    for dm in cand["dense_min"]:
-        plan.set_tuning(iu0, dm, bps0)
-        plan.bin()
-        table.append(((iu0, dm, bps0), _time(step, reps, stream)))
-    best_dm = min(table, key=lambda r: r[1])[0][1]
+    ik0, sm0 = (plan.interp_kernel, plan.step_mode) if full else (None, None)
+    for dm, vk in itertools.product(cand["dense_min"], cand["visit_kernel"]):
+        measure((iu0, dm0 if dm is None else dm, bps0, vk, ik0, sm0))
+    _, dm, _, vk, _, _ = best_cfg()[0]
     for iu, bps in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"]):
-        plan.set_tuning(iu, best_dm, bps)
-        plan.bin()
-        table.append((plan.tuning(), _time(step, reps, stream)))
-    best = min(table, key=lambda r: r[1])[0]
-    plan.set_tuning(*best)
-    plan.bin()
-    # the form of the per-visit kernel, at the best knobs
-    forms = []
-    for form in cand.get("visit_kernel", (0, 1)):
-        plan.visit_kernel = form
-        forms.append((form, _time(step, reps, stream)))
-    best_form, ms = min(forms, key=lambda r: r[1])
-    plan.visit_kernel = best_form
-    out = {"best": best, "ms": ms, "table": table, "visit_kernel": best_form, "visit_kernel_ms": forms}
+        measure((iu, dm, bps, vk, ik0, sm0))
+    if full:
+        iu, dm, bps, vk, _, _ = best_cfg()[0]
+        for ik, sm in itertools.product(cand["interp_kernel"], cand["step_mode"]):
+            measure((iu, dm, bps, vk, ik, sm))
+    cfg, ms = best_cfg()
+    apply(cfg)
+    out = {"best": tuple(plan.tuning()), "ms": ms, "table": table, "config": cfg, "visit_kernel": cfg[3],
+           "interp_kernel": cfg[4], "step_mode": cfg[5]}
     if key is not None:
         _cache[key] = out
     return out
@@ -113,7 +145,8 @@ def autotune_shape(make_plan, shapes=(0, 1), reps=3, candidates=None):
             if best_plan is not None:
                 best_plan.close()
             best_plan, best = plan, {"shape": sh, "ms": res["ms"], "best": res["best"],
-                                     "visit_kernel": res["visit_kernel"]}
+                                     "visit_kernel": res["visit_kernel"], "interp_kernel": res["interp_kernel"],
+                                     "step_mode": res["step_mode"]}
         else:
             plan.close()
     best["per_shape"] = per

@@ -267,9 +267,25 @@ int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, i
 /* Form of the per-visit spread kernel (no reference counterpart; chosen by
  * the autotuner): 0 = the in-tile points of 32 visits flattened over the
  * lanes (default), 1 = one lane per (visit, component) with all components
- * of the tile accumulated at once.  Same results up to FP32 rounding. */
+ * of the tile accumulated at once, 2 = the tile gathered: each lane owns
+ * values of the tile in registers and adds every visit's separable weights
+ * (no atomics).  Same results up to FP32 rounding. */
 int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_visit_kernel(const ibx_plan* plan);
+/* Form of the interpolation (no reference counterpart; chosen by the
+ * autotuner): 1 = markers of dense home tiles interpolated per home unit
+ * (the unit's stencil values loaded once, every marker of the unit summed
+ * from them), the others in chunks of consecutive markers (default); 0 =
+ * every marker in chunks.  Same results: both forms sum in the same order. */
+int ibx_plan_set_interp_kernel(ibx_plan* plan, int form);
+int ibx_plan_get_interp_kernel(const ibx_plan* plan);
+/* How ibx_plan_step orders spread and interpolation after the binning (no
+ * reference counterpart; chosen by the autotuner): 1 = concurrently, the
+ * interpolation on a stream of the plan forked from and joined back to the
+ * caller's stream (default); 0 = one after the other on the caller's
+ * stream.  Same results. */
+int ibx_plan_set_step_mode(ibx_plan* plan, int mode);
+int ibx_plan_get_step_mode(const ibx_plan* plan);
 /* Bytes of device scratch the plan holds. */
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);

@@ -34,7 +34,8 @@ def seam_markers(rng, n, dim):
     return X.reshape(-1)
 
 
-def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, tile_shape=0, visit_kernel=0):
+def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, tile_shape=0, visit_kernel=0,
+             interp_kernel=None):
     ncomp = dim if centering == ibx.SIDE else depth
     shape = list(N)[::-1]
     dx = [1.0 / v for v in N]
@@ -56,7 +57,10 @@ def run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=None, til
     pi = ibx.Plan(mk(uq, U_t), kernel, ibx.MIXED, tile_shape=tile_shape)
     if dense_min is not None:
         ps.set_tuning(dense_min=dense_min)
+        pi.set_tuning(dense_min=dense_min)
     ps.visit_kernel = visit_kernel
+    if interp_kernel is not None:
+        pi.interp_kernel = interp_kernel
     ps.bin()
     ps.spread()
     pi.bin()
@@ -261,10 +265,10 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
     plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED)
     res = tuning.autotune(plan, reps=1, candidates={"dense_min": (0, 32, 1 << 30), "item_units": (32, 256),
                                                     "dense_blocks_per_sm": (1, 2)})
-    assert len(res["table"]) == 3 + 4 and res["visit_kernel"] in (0, 1)
-    assert plan.tuning() == res["best"]
-    assert res["best"] == min(res["table"], key=lambda r: r[1])[0]
-    assert res["ms"] == min(t for _, t in res["visit_kernel_ms"])
+    assert len(res["table"]) == 3 * 3 + 4 and res["visit_kernel"] in (0, 1, 2)
+    assert plan.tuning() == res["best"] and plan.visit_kernel == res["visit_kernel"]
+    cfg, ms = min(res["table"], key=lambda r: r[1])
+    assert res["best"] == cfg[:3] and res["ms"] == ms
     for t in f_t:
         t.zero_()
     plan.bin()
@@ -383,13 +387,15 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim):
     plan.close()
 
 
+@pytest.mark.parametrize("form", [1, 2])
 @pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 2)])
-def test_visit_kernel_lane_form(ibx, oracle, kernel, dim, centering, depth, tile_shape):
-    """The lane-per-(visit, component) form of the per-visit kernel, every
-    marker spread through its visits, against the oracle."""
+def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_shape, form):
+    """The lane-per-(visit, component) form (1) and the tile-gather form (2)
+    of the per-visit kernel, every marker spread through its visits, against
+    the oracle."""
     rng = np.random.default_rng(71 + dim + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     N = [29, 22, 18][:dim] if dim == 3 else [45, 38]
     n = 2500
@@ -399,9 +405,38 @@ def test_visit_kernel_lane_form(ibx, oracle, kernel, dim, centering, depth, tile
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
     f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=1 << 30,
-                            tile_shape=tile_shape, visit_kernel=1)
-    assert ps.visit_kernel == 1
+                            tile_shape=tile_shape, visit_kernel=form)
+    assert ps.visit_kernel == form
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     assert cases.rel_err(U, U_ref) <= MIXED_TOL
     ps.close()
     pi.close()
+
+
+@pytest.mark.parametrize("tile_shape", [0, 1])
+@pytest.mark.parametrize("kernel", KERNEL_NAMES)
+@pytest.mark.parametrize("dim,N", [(2, [52, 35]), (3, [27, 20, 34]), (3, [32, 20, 18])])
+@pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
+@pytest.mark.parametrize("dense_min", [0, 8])
+def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, tile_shape, dense_min):
+    """Interpolation of dense-homed markers per home unit, and of the others
+    in chunks with aligned vector row reads where N0 is a multiple of 4, sums
+    in the same order as the chunked form: bit-identical results (every tile
+    dense, then a mix), both within the bar of the oracle."""
+    rng = np.random.default_rng(91 + N[0] + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
+    n = 2000
+    X = seam_markers(rng, n, dim)
+    ncomp = dim if centering == 1 else depth
+    F = rng.standard_normal(n * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
+    got = []
+    for form in (1, 0):
+        f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min,
+                                tile_shape=tile_shape, interp_kernel=form)
+        assert pi.interp_kernel == form
+        assert cases.rel_err(U, U_ref) <= MIXED_TOL
+        got.append(U)
+        ps.close()
+        pi.close()
+    assert np.array_equal(got[0], got[1])
