@@ -67,16 +67,27 @@ class BatchedProblems:
                                                [0.0] * dim, [1.0] * dim, q, self.X[a:b], Q[a:b])
             sp.append(mk(fq, self.F))
             ip.append(mk(uq, self.U))
-        make = lambda shape: ibx.Plan(sp, kernel, ibx.MIXED, interp_problems=ip, tile_shape=shape)
+        self._make = lambda shape: ibx.Plan(sp, kernel, ibx.MIXED, interp_problems=ip, tile_shape=shape)
         self.tuning = None
-        if tune:
-            from . import tuning
-
-            self.plan, self.tuning = tuning.autotune_shape(make, reps=tune_reps)
-            self.f.zero_()
-        else:
-            self.plan = make(0)
+        self.plan = None
         self.graph = None
+        if tune:
+            self.autotune(tune_reps)
+        else:
+            self.plan = self._make(0)
+
+    def autotune(self, reps=3):
+        """Tune the plan (tile shape and knobs, ``tuning.autotune_shape``) on
+        the current contents of the buffers, which should hold representative
+        forces and velocities: the kernels skip zero contributions.  The
+        spread target ``f`` is zeroed afterwards; a captured graph is dropped."""
+        from . import tuning
+
+        if self.plan is not None:
+            self.plan.close()
+        self.graph = None
+        self.plan, self.tuning = tuning.autotune_shape(self._make, reps=reps)
+        self.f.zero_()
 
     # -- views ------------------------------------------------------------
     def grid(self, field, k):

@@ -192,11 +192,15 @@ base_key(const Rec& R)
     return R.key;
 }
 
-// Lanes of the active set that share both the tile and the stencil key.
+// Lanes of the active set that share both the tile and the stencil key,
+// split into groups of at most cap lanes (by rank within the group).
 __device__ __forceinline__ unsigned
-unit_group(unsigned act, int tile, unsigned long long key)
+unit_group(unsigned act, int tile, unsigned long long key, int cap = 32)
 {
-    return __match_any_sync(act, tile) & __match_any_sync(act, key);
+    const unsigned grp = __match_any_sync(act, tile) & __match_any_sync(act, key);
+    if (cap >= 32) return grp;
+    const int sub = __popc(grp & ((1u << (threadIdx.x & 31)) - 1)) / cap;
+    return grp & __match_any_sync(act, sub);
 }
 
 // Phase 0: one thread per marker derives the record (exact stencil bases
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
     bool lead = false;
     if (valid)
     {
-        const unsigned grp = unit_group(act, ht, key);
+        const unsigned grp = unit_group(act, ht, key, D.unit_cap);
         lead = (threadIdx.x & 31) == __ffs(grp) - 1;
     }
     agg_count(D.hcount, ht, valid);
@@ -310,6 +314,13 @@ template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
 {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    // Dense-tile spread work items: a home tile with more than dense_min
+    // markers and u home units gets ceil(u / item_units) items.
+    for (long long t = g; t < D.n_tiles; t += (long long)gridDim.x * blockDim.x)
+    {
+        const int u = D.hucount[t + 1] - D.hucount[t];
+        D.items[t] = dense_home(D, (int)t) ? (u + D.item_units - 1) / D.item_units : 0;
+    }
     bool valid = g < D.n_markers;
     const int ht = valid ? D.home_tile[g] : -1;
     valid = valid && ht >= 0;
@@ -327,7 +338,7 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
         const unsigned act = __ballot_sync(0xffffffffu, valid);
         if (valid)
         {
-            const unsigned grp = unit_group(act, ht, key);
+            const unsigned grp = unit_group(act, ht, key, D.unit_cap);
             const int pos = place_group(grp, ht, D.hcursor, D.hcount, D.hucursor, D.hucount, D.home_units);
             D.home_list[pos] = (int)g;
             D.hrec[pos] = R;
@@ -438,16 +449,6 @@ __global__ void scan_add(int* data, int n, const int* block_offsets, int nb)
     if (i < n) data[(long long)blockIdx.y * n + i] += block_offsets[blockIdx.y * nb + i / SCAN_ITEMS];
 }
 
-// Dense-tile spread work items: a home tile with more than dense_min markers
-// and u home units gets ceil(u / item_units) items.
-__global__ void items_count(const DevPlan D)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= D.n_tiles) return;
-    const int u = D.hucount[t + 1] - D.hucount[t];
-    D.items[t] = dense_home(D, t) ? (u + D.item_units - 1) / D.item_units : 0;
-}
-
 __global__ void items_fill(const DevPlan D)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,7 +462,7 @@ int
 exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s)
 {
     const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
-    if (nb > SCAN_ITEMS) return IBX_E_TOO_LARGE; // more than 4M entries
+    if (nb > SCAN_ITEMS || (long long)nb * count > SCAN_TMP_INTS) return IBX_E_TOO_LARGE; // more than 4M entries
     scan_blocks<<<dim3(nb, count), SCAN_BLOCK, 0, s>>>(data, n, tmp, nb);
     if (nb > 1)
     {
@@ -474,13 +475,10 @@ exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s)
 }
 
 int
-launch_items(const DevPlan& D, cudaStream_t s, bool fill)
+launch_items_fill(const DevPlan& D, cudaStream_t s)
 {
     const int blocks = (D.n_tiles + 255) / 256;
-    if (fill)
-        items_fill<<<blocks, 256, 0, s>>>(D);
-    else
-        items_count<<<blocks, 256, 0, s>>>(D);
+    items_fill<<<blocks, 256, 0, s>>>(D);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
@@ -531,12 +529,10 @@ bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t 
     if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
     int rc = launch_bin(dim, kernel, D, s, 0);
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
-    if (!rc) rc = launch_bin(dim, kernel, D, s, 1);
-    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 2, scan_tmp, s); // vcount, ucount
+    if (!rc) rc = launch_bin(dim, kernel, D, s, 1);                 // also counts the work items
+    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 3, scan_tmp, s); // vcount, ucount, items
     if (!rc) rc = launch_bin(dim, kernel, D, s, 2);
-    if (!rc) rc = launch_items(D, s, false);
-    if (!rc) rc = exclusive_scan(D.items, nt + 1, 1, scan_tmp, s);
-    if (!rc) rc = launch_items(D, s, true);
+    if (!rc) rc = launch_items_fill(D, s);
     return rc;
 }
 

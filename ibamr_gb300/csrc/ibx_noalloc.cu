@@ -138,7 +138,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     z.n_tiles = nt;
     z.visit_cap = nm * (dim == 3 ? 8 : 4);
     z.item_cap = nt + nm / 10 + 1;
-    DevPlan D;
+    DevPlan D{};
     if (carve_plan(z, nullptr, D).bytes > NOALLOC_SCRATCH_BYTES) return IBX_E_TOO_LARGE;
 
     void* base = nullptr;

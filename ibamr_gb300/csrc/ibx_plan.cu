@@ -97,7 +97,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     const size_t o_home_units = take(sizeof(int2) * nm);
     const size_t o_units = take(sizeof(int2) * z.visit_cap);
     c.o_status = take(sizeof(int) * 4);
-    const size_t o_scan = take(sizeof(int) * 4096);
+    const size_t o_scan = take(sizeof(int) * SCAN_TMP_INTS);
     c.bytes = off;
     c.scan_tmp = nullptr;
     if (!b) return c;
@@ -116,11 +116,11 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.hucount = counts + (nt + 1);
     D.vcount = counts + 2 * (nt + 1);
     D.ucount = counts + 3 * (nt + 1);
-    D.hcursor = counts + 4 * (nt + 1);
+    D.items = counts + 4 * (nt + 1);
+    D.hcursor = counts + 5 * (nt + 1);
     D.hucursor = D.hcursor + nt;
     D.vcursor = D.hucursor + nt;
     D.ucursor = D.vcursor + nt;
-    D.items = D.ucursor + nt;
     D.home_list = reinterpret_cast<int*>(b + o_home_list);
     D.visit_list = reinterpret_cast<int*>(b + o_visit);
     D.n_visit_cap = z.visit_cap;
@@ -130,7 +130,9 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.n_item_cap = (int)z.item_cap;
     D.item_units = ITEM_UNITS;
     D.dense_min = DENSE_MIN;
-    D.dense_interp = 1;
+    D.interp_form = 0;
+    D.visit_kernel = 2;
+    D.unit_cap = 32;
     D.tile_shape = z.tile_shape;
     D.dense_blocks_per_sm = 2;
     D.status = reinterpret_cast<int*>(b + c.o_status);
@@ -262,8 +264,6 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         }
         P.vec4 = P.N[0] % 4 == 0;
         for (int c = 0; c < ncomp; ++c) P.vec4 = P.vec4 && (reinterpret_cast<unsigned long long>(P.q[c]) & 15) == 0;
-        P.vec4i = P.N[0] % 4 == 0;
-        for (int c = 0; c < ncomp; ++c) P.vec4i = P.vec4i && (reinterpret_cast<unsigned long long>(P.qi[c]) & 15) == 0;
         P.tile0 = toffs[p];
         P.marker0 = moffs[p];
         if ((long long)toffs[p] + ntiles > 0x3fffffffLL) return IBX_E_TOO_LARGE;
@@ -275,7 +275,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     // Dense work items: at most one per tile plus one per MIN_ITEM_UNITS units.
     const long long item_cap = toffs[n_problems] + moffs[n_problems] / (MIN_ITEM_UNITS / 3) + 1;
     if (item_cap > 0x7fffffffLL || visit_cap > 0x7fffffffLL) return IBX_E_TOO_LARGE;
-    ibx_plan* plan = new (std::nothrow) ibx_plan;
+    ibx_plan* plan = new (std::nothrow) ibx_plan();
     if (!plan) return IBX_E_OOM;
     std::memset(plan, 0, sizeof(*plan));
     plan->dim = dim;
@@ -450,6 +450,20 @@ ibx_plan_get_visit_kernel(const ibx_plan* plan)
 }
 
 int
+ibx_plan_set_unit_cap(ibx_plan* plan, int cap)
+{
+    if (!plan || cap < 1 || cap > 32) return IBX_E_ARG;
+    plan->D.unit_cap = cap;
+    return IBX_OK;
+}
+
+int
+ibx_plan_get_unit_cap(const ibx_plan* plan)
+{
+    return plan ? plan->D.unit_cap : -1;
+}
+
+int
 ibx_plan_set_step_mode(ibx_plan* plan, int mode)
 {
     if (!plan || mode < 0 || mode > 1) return IBX_E_ARG;
@@ -467,14 +481,14 @@ int
 ibx_plan_set_interp_kernel(ibx_plan* plan, int form)
 {
     if (!plan || form < 0 || form > 1) return IBX_E_ARG;
-    plan->D.dense_interp = form;
+    plan->D.interp_form = form;
     return IBX_OK;
 }
 
 int
 ibx_plan_get_interp_kernel(const ibx_plan* plan)
 {
-    return plan ? plan->D.dense_interp : -1;
+    return plan ? plan->D.interp_form : -1;
 }
 
 int

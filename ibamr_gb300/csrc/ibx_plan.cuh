@@ -99,7 +99,6 @@ struct PlanProb
     FixedDim fx[3];
     float inv_vol;     // 1/(dx0*dx1[*dx2]) rounded to FP32
     int vec4;          // N[0] % 4 == 0 and every spread target 16-byte aligned
-    int vec4i;         // N[0] % 4 == 0 and every interpolation source 16-byte aligned
     const double* X;
     void* Q;           // spread source
     void* q[3];        // spread target, one array per component (side axis or cell depth)
@@ -124,8 +123,8 @@ struct DevPlan
     Rec* hrec;        // [n_markers], home-tile order (same order as home_list)
     int* home_tile;   // [n_markers]
     // Counters (zeroed together each step; the *count arrays are scanned in
-    // place into start offsets; hcount/hucount and vcount/ucount are
-    // adjacent so that each pair is scanned by one launch).
+    // place into start offsets; hcount/hucount, then vcount/ucount/items,
+    // are adjacent so that each group is scanned by one launch).
     int* hcount;      // [n_tiles+1] markers per home tile
     int* hucount;     // [n_tiles+1] home units per tile
     int* vcount;      // [n_tiles+1] visits per tile (sparse-homed markers only)
@@ -150,12 +149,18 @@ struct DevPlan
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
     int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component)
-    int dense_interp; // 1: dense-homed markers interpolated per home unit
+    int interp_form;  // 1: dense-homed markers interpolated per home unit, 0: all in chunks
+    int unit_cap;     // most markers per home unit (1..32)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
 
-// Number of ints of the counter block starting at hcount.
+// Block sums of the exclusive scans: up to 3 arrays of up to 2048 blocks.
+constexpr int SCAN_TMP_INTS = 3 * 2048;
+
+// Number of ints of the counter block starting at hcount: hcount, hucount,
+// vcount, ucount and items ([n_tiles + 1] each, adjacent so that they scan
+// together), then the four cursors ([n_tiles] each).
 __host__ __device__ inline size_t
 counter_ints(int n_tiles)
 {
@@ -330,7 +335,7 @@ int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 // Exclusive scans of `count` arrays of n ints laid out back to back; tmp
 // holds count * 2048 ints.
 int exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s);
-int launch_items(const DevPlan& D, cudaStream_t s, bool fill);
+int launch_items_fill(const DevPlan& D, cudaStream_t s);
 int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
 int launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s);
 

@@ -94,6 +94,8 @@ def lib():
             L.ibx_plan_get_interp_kernel.argtypes = [ctypes.c_void_p]
             L.ibx_plan_set_step_mode.argtypes = [ctypes.c_void_p, ctypes.c_int]
             L.ibx_plan_get_step_mode.argtypes = [ctypes.c_void_p]
+            L.ibx_plan_set_unit_cap.argtypes = [ctypes.c_void_p, ctypes.c_int]
+            L.ibx_plan_get_unit_cap.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -363,6 +365,17 @@ class Plan:
         rc = lib().ibx_plan_set_step_mode(self.h, int(mode))
         if rc:
             raise IbxError(rc, "ibx_plan_set_step_mode")
+
+    @property
+    def unit_cap(self):
+        """Most markers per home unit (see ibx_plan_set_unit_cap)."""
+        return lib().ibx_plan_get_unit_cap(self.h)
+
+    @unit_cap.setter
+    def unit_cap(self, cap):
+        rc = lib().ibx_plan_set_unit_cap(self.h, int(cap))
+        if rc:
+            raise IbxError(rc, "ibx_plan_set_unit_cap")
 
     def tuning(self):
         """(item_units, dense_min, dense_blocks_per_sm)."""

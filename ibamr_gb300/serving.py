@@ -43,7 +43,7 @@ def plan_bytes_estimate(dim, N, n_markers):
     b += visit_cap * (4 + 8)                    # visit list, visit units
     b += 4 * (9 * tiles + 5)                    # counters
     b += 4 * (tiles + n_markers // 10 + 1)      # dense work items
-    b += 16 * 1024 + 14 * 256                   # descriptors, scan scratch, alignment
+    b += 4 * 3 * 2048 + 4096 + 14 * 256         # scan scratch, descriptors, alignment
     return b
 
 

@@ -8,8 +8,9 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   the two spread kernels);
 * ``visit_kernel``: the form of the per-visit spread kernel (points
   flattened over lanes, lane per visit, or the tile gathered in registers);
-* ``item_units`` and ``dense_blocks_per_sm``: home units per CTA work item
-  and CTAs per SM of the dense-tile kernel;
+* ``item_units``, ``dense_blocks_per_sm`` and ``unit_cap``: home units per
+  CTA work item, CTAs per SM of the dense-tile kernel, and most markers per
+  home unit (a unit is spread by one thread per component);
 * ``interp_kernel``: dense-homed markers interpolated per home unit, or all
   markers in chunks;
 * ``step_mode``: spread and interpolation concurrent or one after the other
@@ -37,8 +38,9 @@ DEFAULT_CANDIDATES = {
     "item_units": (32, 64, 128, 256),
     "dense_blocks_per_sm": (1, 2, 4),
     "visit_kernel": (0, 1, 2),
-    "interp_kernel": (1, 0),
+    "interp_kernel": (0, 1),
     "step_mode": (1, 0),
+    "unit_cap": (32, 16, 8),
 }
 
 _cache = {}
@@ -65,13 +67,13 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     The search runs in three stages, each at the best setting so far: the
     split between the two spread kernels (``dense_min``) jointly with the
     per-visit kernel form; the dense-kernel knobs (``item_units``,
-    ``dense_blocks_per_sm``); for plans with their own interpolation targets,
+    ``dense_blocks_per_sm``, ``unit_cap``); for plans with their own interpolation targets,
     the interpolation form jointly with the step mode (concurrent or serial
     spread and interpolation).  Returns {"best": (item_units, dense_min,
     dense_blocks_per_sm), "visit_kernel": form, "interp_kernel": form or
-    None, "step_mode": mode or None, "ms": t, "table": [((item_units,
-    dense_min, dense_blocks_per_sm, visit_kernel, interp_kernel, step_mode),
-    ms), ...]}, t being the time of the applied setting.  With ``key`` the
+    None, "step_mode": mode or None, "unit_cap": cap, "ms": t, "table":
+    [((item_units, dense_min, dense_blocks_per_sm, visit_kernel,
+    interp_kernel, step_mode, unit_cap), ms), ...]}, t being the time of the applied setting.  With ``key`` the
     result is cached for this process and later calls with the same key only
     apply it."""
     import torch
@@ -79,8 +81,9 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     full = include_bin and getattr(plan, "separate_interp", False)
 
     def apply(cfg):
-        iu, dm, bps, vk, ik, sm = cfg
+        iu, dm, bps, vk, ik, sm, cap = cfg
         plan.set_tuning(iu, dm, bps)
+        plan.unit_cap = cap
         plan.visit_kernel = vk
         if full:
             plan.interp_kernel = ik
@@ -113,20 +116,21 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
         return min(table, key=lambda r: r[1])
 
     iu0, dm0, bps0 = plan.tuning()
+    cap0 = plan.unit_cap
     ik0, sm0 = (plan.interp_kernel, plan.step_mode) if full else (None, None)
     for dm, vk in itertools.product(cand["dense_min"], cand["visit_kernel"]):
-        measure((iu0, dm0 if dm is None else dm, bps0, vk, ik0, sm0))
-    _, dm, _, vk, _, _ = best_cfg()[0]
-    for iu, bps in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"]):
-        measure((iu, dm, bps, vk, ik0, sm0))
+        measure((iu0, dm0 if dm is None else dm, bps0, vk, ik0, sm0, cap0))
+    _, dm, _, vk, _, _, _ = best_cfg()[0]
+    for iu, bps, cap in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"], cand["unit_cap"]):
+        measure((iu, dm, bps, vk, ik0, sm0, cap))
     if full:
-        iu, dm, bps, vk, _, _ = best_cfg()[0]
+        iu, dm, bps, vk, _, _, cap = best_cfg()[0]
         for ik, sm in itertools.product(cand["interp_kernel"], cand["step_mode"]):
-            measure((iu, dm, bps, vk, ik, sm))
+            measure((iu, dm, bps, vk, ik, sm, cap))
     cfg, ms = best_cfg()
     apply(cfg)
     out = {"best": tuple(plan.tuning()), "ms": ms, "table": table, "config": cfg, "visit_kernel": cfg[3],
-           "interp_kernel": cfg[4], "step_mode": cfg[5]}
+           "interp_kernel": cfg[4], "step_mode": cfg[5], "unit_cap": cfg[6]}
     if key is not None:
         _cache[key] = out
     return out
@@ -146,7 +150,7 @@ def autotune_shape(make_plan, shapes=(0, 1), reps=3, candidates=None):
                 best_plan.close()
             best_plan, best = plan, {"shape": sh, "ms": res["ms"], "best": res["best"],
                                      "visit_kernel": res["visit_kernel"], "interp_kernel": res["interp_kernel"],
-                                     "step_mode": res["step_mode"]}
+                                     "step_mode": res["step_mode"], "unit_cap": res["unit_cap"]}
         else:
             plan.close()
     best["per_shape"] = per

@@ -266,17 +266,18 @@ int ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense
 int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, int* dense_blocks_per_sm);
 /* Form of the per-visit spread kernel (no reference counterpart; chosen by
  * the autotuner): 0 = the in-tile points of 32 visits flattened over the
- * lanes (default), 1 = one lane per (visit, component) with all components
- * of the tile accumulated at once, 2 = the tile gathered: each lane owns
- * values of the tile in registers and adds every visit's separable weights
- * (no atomics).  Same results up to FP32 rounding. */
+ * lanes, 1 = one lane per (visit, component) with all components of the
+ * tile accumulated at once, 2 = the tile gathered: each lane owns values of
+ * the tile in registers and adds every visit's separable weights, no
+ * atomics (default).  Same results up to FP32 rounding. */
 int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_visit_kernel(const ibx_plan* plan);
 /* Form of the interpolation (no reference counterpart; chosen by the
  * autotuner): 1 = markers of dense home tiles interpolated per home unit
  * (the unit's stencil values loaded once, every marker of the unit summed
- * from them), the others in chunks of consecutive markers (default); 0 =
- * every marker in chunks.  Same results: both forms sum in the same order. */
+ * from them), the others in chunks of consecutive markers; 0 = every marker
+ * in chunks (default).  Both forms sum in the same order: identical
+ * results. */
 int ibx_plan_set_interp_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_interp_kernel(const ibx_plan* plan);
 /* How ibx_plan_step orders spread and interpolation after the binning (no
@@ -286,6 +287,13 @@ int ibx_plan_get_interp_kernel(const ibx_plan* plan);
  * stream.  Same results. */
 int ibx_plan_set_step_mode(ibx_plan* plan, int mode);
 int ibx_plan_get_step_mode(const ibx_plan* plan);
+/* Most markers per home unit (1..32; no reference counterpart; chosen by the
+ * autotuner).  A home unit is a run of markers of one home tile that share
+ * every stencil base, spread by one thread per component of the dense-tile
+ * kernel; shorter units balance the threads of a warp at the cost of more
+ * merges.  Default 32.  Takes effect at the next ibx_plan_bin. */
+int ibx_plan_set_unit_cap(ibx_plan* plan, int cap);
+int ibx_plan_get_unit_cap(const ibx_plan* plan);
 /* Bytes of device scratch the plan holds. */
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);

@@ -264,7 +264,7 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
                                        [1.0] * 3, q, X_t, Q)
     plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED)
     res = tuning.autotune(plan, reps=1, candidates={"dense_min": (0, 32, 1 << 30), "item_units": (32, 256),
-                                                    "dense_blocks_per_sm": (1, 2)})
+                                                    "dense_blocks_per_sm": (1, 2), "unit_cap": (32,)})
     assert len(res["table"]) == 3 * 3 + 4 and res["visit_kernel"] in (0, 1, 2)
     assert plan.tuning() == res["best"] and plan.visit_kernel == res["visit_kernel"]
     cfg, ms = min(res["table"], key=lambda r: r[1])
@@ -419,10 +419,9 @@ def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_sha
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
 @pytest.mark.parametrize("dense_min", [0, 8])
 def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, tile_shape, dense_min):
-    """Interpolation of dense-homed markers per home unit, and of the others
-    in chunks with aligned vector row reads where N0 is a multiple of 4, sums
-    in the same order as the chunked form: bit-identical results (every tile
-    dense, then a mix), both within the bar of the oracle."""
+    """Both interpolation forms (dense-homed markers per home unit or in
+    chunks) sum in the same order: bit-identical results (every tile dense,
+    then a mix), both within the bar of the oracle."""
     rng = np.random.default_rng(91 + N[0] + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     n = 2000
     X = seam_markers(rng, n, dim)
@@ -439,4 +438,39 @@ def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, t
         got.append(U)
         ps.close()
         pi.close()
-    assert np.array_equal(got[0], got[1])
+    for g in got[:-1]:
+        assert np.array_equal(g, got[-1])
+
+
+@pytest.mark.parametrize("cap", [1, 5, 32])
+@pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "PIECEWISE_LINEAR"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_unit_cap(ibx, oracle, kernel, dim, cap):
+    """Home units capped at 1, 5 and 32 markers (every tile dense): the
+    counting sort stays exact and the spread and interpolation stay within
+    the bar of the oracle."""
+    rng = np.random.default_rng(301 + dim + 7 * cap + 100 * KERNEL_NAMES.index(kernel))
+    N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
+    n = 3000
+    # clustered markers: long runs of equal stencil bases
+    X = (rng.uniform(0.4, 0.45, size=(n, dim)) + rng.uniform(0, 1e-3, size=(n, dim))).reshape(-1)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=1)
+    X_t = torch.tensor(X, device="cuda")
+    f_t = [torch.zeros(N[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED, interp_problems=[mk(u_t, U_t)])
+    plan.set_tuning(dense_min=0)
+    plan.unit_cap = cap
+    assert plan.unit_cap == cap
+    plan.step()
+    torch.cuda.synchronize()
+    f = np.stack([t.double().cpu().numpy() for t in f_t])
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
+    plan.close()
