@@ -655,6 +655,30 @@ struct GatherOccupancy
     static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 3;
 };
 
+// Two FP32 lanes in one 64-bit register: {lo, hi} = {first, second}.
+__device__ __forceinline__ unsigned long long
+pack2(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ void
+unpack2(unsigned long long r, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+
+// d = a * b + c on both FP32 lanes, each rounded once (as fmaf).
+__device__ __forceinline__ unsigned long long
+fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::value)
     spread_visits_gather(const DevPlan D)
@@ -663,14 +687,19 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
     using T = TileT<DIM, SH>;
     using GL = GatherLayout<DIM, SH>;
     constexpr int CPL = GL::CPL, SX = GL::SX, NR = GL::NR, SS = GL::SS;
+    constexpr int SP = SX / 2; // value pairs per lane row
     extern __shared__ float sm[]; // [GATHER_WARPS][32][SS]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float* slots = sm + warp * 32 * SS;
     float* mine = slots + lane * SS;
-    // this lane's values: rows r0 .. r0 + NR - 1 (row = y + E1 * z), x in [xs, xs + SX)
+    // This lane's values: NR consecutive rows y0 .. y0 + NR - 1 of plane z
+    // (rows are y + E1 * z; NR and E1 are even or NR is 1), x in [xs, xs + SX).
     const int first = lane * CPL;
     const int r0 = first / T::E0;
     const int xs = first % T::E0;
+    const int y0 = r0 % T::E1;
+    const int z0 = r0 / T::E1;
+    static_assert(NR == 1 || (NR == 2 && T::E1 % 2 == 0), "a lane's rows share their plane");
     for (int t = blockIdx.x * GATHER_WARPS + warp; t < D.n_tiles; t += gridDim.x * GATHER_WARPS)
     {
         const int vbeg = D.vcount[t];
@@ -681,6 +710,16 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
         int org[3];
         tile_origin<DIM, SH>(P, t - P.tile0, org);
         const float* Qf = static_cast<const float*>(P.Q);
+        // A tile with at most 32 visits keeps each lane's visit in registers
+        // for every component.
+        const bool one = vend - vbeg <= 32;
+        int gk = 0;
+        Rec Rk;
+        if (one && lane < vend - vbeg)
+        {
+            gk = D.visit_list[vbeg + lane];
+            Rk = D.rec[gk];
+        }
         for (int c = 0; c < P.ncomp; ++c)
         {
             float hi[CPL], lo[CPL];
@@ -694,8 +733,8 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
                 for (int i = 0; i < SS / 4; ++i) reinterpret_cast<float4*>(mine)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (lane < nb)
                 {
-                    const int g = D.visit_list[b0 + lane];
-                    const Rec R = D.rec[g];
+                    const int g = one ? gk : D.visit_list[b0 + lane];
+                    const Rec R = one ? Rk : D.rec[g];
                     const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d)
@@ -715,42 +754,61 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
                     }
                 }
                 __syncwarp();
-                // -- the batch's contraction into this lane's values
-                float acc[CPL];
+                // -- the batch's contraction into this lane's values, two
+                //    x-values per packed multiply-add
+                unsigned long long acc[NR][SP];
 #pragma unroll
-                for (int i = 0; i < CPL; ++i) acc[i] = 0.f;
+                for (int k = 0; k < NR; ++k)
+#pragma unroll
+                    for (int j = 0; j < SP; ++j) acc[k][j] = 0ull;
                 for (int m = 0; m < nb; ++m)
                 {
                     const float* sv = slots + m * SS;
-                    float bx[SX];
+                    unsigned long long bx[SP];
 #pragma unroll
-                    for (int i = 0; i < SX / 4; ++i)
+                    for (int j = 0; j < SP / 2; ++j)
                     {
-                        const float4 q4 = *reinterpret_cast<const float4*>(sv + xs + 4 * i);
-                        bx[4 * i] = q4.x;
-                        bx[4 * i + 1] = q4.y;
-                        bx[4 * i + 2] = q4.z;
-                        bx[4 * i + 3] = q4.w;
+                        const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(sv + xs + 4 * j);
+                        bx[2 * j] = q2.x;
+                        bx[2 * j + 1] = q2.y;
                     }
+                    float ay[NR];
+                    if (NR == 2)
+                    {
+                        const float2 y2 = *reinterpret_cast<const float2*>(sv + T::E0 + y0);
+                        ay[0] = y2.x;
+                        ay[NR - 1] = y2.y;
+                    }
+                    else
+                        ay[0] = sv[T::E0 + y0];
+                    const float az = DIM == 3 ? sv[T::E0 + T::E1 + z0] : 1.f;
 #pragma unroll
                     for (int k = 0; k < NR; ++k)
                     {
-                        const int r = r0 + k;
-                        const float a = DIM == 3 ? sv[T::E0 + r % T::E1] * sv[T::E0 + T::E1 + r / T::E1]
-                                                 : sv[T::E0 + r];
+                        const float a = DIM == 3 ? ay[k] * az : ay[k];
+                        const unsigned long long aa = pack2(a, a);
 #pragma unroll
-                        for (int i = 0; i < SX; ++i) acc[k * SX + i] = fmaf(bx[i], a, acc[k * SX + i]);
+                        for (int j = 0; j < SP; ++j) acc[k][j] = fma2(bx[j], aa, acc[k][j]);
                     }
                 }
                 // -- fold the batch sums into the double-FP32 pair
 #pragma unroll
-                for (int i = 0; i < CPL; ++i)
-                {
-                    const float s = hi[i] + acc[i];
-                    const float bp = s - hi[i];
-                    lo[i] += (hi[i] - (s - bp)) + (acc[i] - bp);
-                    hi[i] = s;
-                }
+                for (int k = 0; k < NR; ++k)
+#pragma unroll
+                    for (int j = 0; j < SP; ++j)
+                    {
+                        float av[2];
+                        unpack2(acc[k][j], av[0], av[1]);
+#pragma unroll
+                        for (int e = 0; e < 2; ++e)
+                        {
+                            const int i = k * SX + 2 * j + e;
+                            const float s2 = hi[i] + av[e];
+                            const float bp = s2 - hi[i];
+                            lo[i] += (hi[i] - (s2 - bp)) + (av[e] - bp);
+                            hi[i] = s2;
+                        }
+                    }
                 __syncwarp();
             }
             // -- q += hi + lo for this lane's values
@@ -758,9 +816,8 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
 #pragma unroll
             for (int k = 0; k < NR; ++k)
             {
-                const int r = r0 + k;
-                const int y = org[1] + r % T::E1;
-                const int z = DIM == 3 ? org[2] + r / T::E1 : 0;
+                const int y = org[1] + y0 + k;
+                const int z = DIM == 3 ? org[2] + z0 : 0;
                 if (y >= P.N[1] || (DIM == 3 && z >= P.N[2])) continue;
                 const int x0 = org[0] + xs;
                 const long long o = x0 + (long long)P.N[0] * (y + (long long)P.N[1] * z);
@@ -794,6 +851,7 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
         }
     }
 }
+
 } // namespace
 
 namespace
