@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=float, default=0.1, help="fraction of markers for the CPU baseline")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
+    ap.add_argument("--setting", default=None,
+                    help="fixed plan setting k=v,... as printed under tuning.setting (skips the autotuner)")
     ap.add_argument("--workload", default="helices", choices=["helices", "batched", "serving"],
                     help="helices: 2M markers on 256^3 (default); batched: 512 independent 2D problems in one "
                          "CUDA graph; serving: Poisson request stream over resident simulations")
@@ -265,13 +267,18 @@ def run_ours(args):
         return ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)],
                         tile_shape=shape)
 
+    from ibamr_gb300 import tuning
+
     tuned = None
-    if args.no_tune:
+    if args.setting:
+        fixed = tuning.parse_setting(args.setting)
+        plan = make_plan(fixed.get("tile_shape", 0))
+        tuning.apply_setting(plan, fixed)
+    elif args.no_tune:
         plan = make_plan(0)
     else:
-        from ibamr_gb300 import tuning
-
         plan, tuned = tuning.autotune_shape(make_plan)
+    setting = tuning.setting_string(tuning.setting_of(plan))
 
     def step():
         plan.step()  # bin, then spread and interpolate concurrently
@@ -409,13 +416,12 @@ def run_ours(args):
             "plain_fp64": {"value": n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
-            "tuning": None if tuned is None else {
-                "tile_shape": tuned["shape"], "tile_edges": list(plan_tile_edges),
-                "visit_kernel": tuned["visit_kernel"], "interp_kernel": tuned.get("interp_kernel"),
-                "step_mode": tuned.get("step_mode"), "unit_cap": tuned.get("unit_cap"),
-                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
-                "tuned_step_ms": tuned["ms"],
-                "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
+            "tuning": {
+                "setting": setting, "tile_edges": list(plan_tile_edges),
+                "source": "autotuner" if tuned is not None else "fixed" if args.setting else "library defaults",
+                "tuned_step_ms": None if tuned is None else tuned["ms"],
+                "per_shape": None if tuned is None else {
+                    str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
         }
@@ -495,8 +501,13 @@ def run_batched(args):
     gen = torch.Generator(device=dev)
     gen.manual_seed(workloads.SEED + 41)
     B.u.copy_(torch.randn(B.u.numel(), generator=gen, device=dev))
-    if not args.no_tune:
+    from ibamr_gb300 import tuning
+
+    if args.setting:
+        B.configure(tuning.parse_setting(args.setting))
+    elif not args.no_tune:
         B.autotune()  # on the benchmark's own forces and velocities
+    setting = tuning.setting_string(tuning.setting_of(B.plan))
     stream = torch.cuda.current_stream()
 
     # kernels per step, counted on an eager step
@@ -613,12 +624,11 @@ def run_batched(args):
             "plain_fp64": {"value": nm / (ms_plain * 1e-3), "ms_per_step": ms_plain},
             "mixed_vs_plain": ms_plain / ms,
             "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
-            "tuning": None if tuned is None else {
-                "tile_shape": tuned["shape"], "visit_kernel": tuned["visit_kernel"],
-                "interp_kernel": tuned.get("interp_kernel"), "step_mode": tuned.get("step_mode"),
-                "unit_cap": tuned.get("unit_cap"),
-                "best": dict(zip(("item_units", "dense_min", "dense_blocks_per_sm"), tuned["best"])),
-                "per_shape": {str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
+            "tuning": {
+                "setting": setting,
+                "source": "autotuner" if tuned is not None else "fixed" if args.setting else "library defaults",
+                "per_shape": None if tuned is None else {
+                    str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * args.steps,
             "clocks": clocks,
         }

@@ -76,6 +76,17 @@ class BatchedProblems:
         else:
             self.plan = self._make(0)
 
+    def configure(self, setting):
+        """Use a fixed setting (``tuning.parse_setting``): a plan of its tile
+        shape with its knobs; a captured graph is dropped."""
+        from . import tuning
+
+        if self.plan is not None:
+            self.plan.close()
+        self.graph = None
+        self.plan = self._make(setting.get("tile_shape", 0))
+        tuning.apply_setting(self.plan, setting)
+
     def autotune(self, reps=3):
         """Tune the plan (tile shape and knobs, ``tuning.autotune_shape``) on
         the current contents of the buffers, which should hold representative

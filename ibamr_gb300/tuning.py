@@ -155,3 +155,44 @@ def autotune_shape(make_plan, shapes=(0, 1), reps=3, candidates=None):
             plan.close()
     best["per_shape"] = per
     return best_plan, best
+
+
+KNOBS = ("item_units", "dense_min", "dense_blocks_per_sm", "visit_kernel", "interp_kernel", "step_mode", "unit_cap")
+
+
+def setting_of(plan):
+    """The plan's current setting: tile shape and every knob, as a dict."""
+    iu, dm, bps = plan.tuning()
+    return {"tile_shape": plan.tile_shape[0], "item_units": iu, "dense_min": dm, "dense_blocks_per_sm": bps,
+            "visit_kernel": plan.visit_kernel, "interp_kernel": plan.interp_kernel, "step_mode": plan.step_mode,
+            "unit_cap": plan.unit_cap}
+
+
+def setting_string(setting):
+    """``k=v,...`` form of a setting (the inverse of ``parse_setting``)."""
+    return ",".join("%s=%d" % (k, setting[k]) for k in ("tile_shape",) + KNOBS if k in setting)
+
+
+def parse_setting(text):
+    """Setting dict from ``k=v,...`` (keys: tile_shape and the knobs)."""
+    out = {}
+    for part in text.split(","):
+        if not part:
+            continue
+        k, v = part.split("=")
+        if k not in ("tile_shape",) + KNOBS:
+            raise ValueError("unknown plan knob %r" % k)
+        out[k] = int(v)
+    return out
+
+
+def apply_setting(plan, setting):
+    """Apply the knobs of a setting to a plan (the tile shape is chosen when
+    the plan is created and must match)."""
+    if "tile_shape" in setting and setting["tile_shape"] != plan.tile_shape[0]:
+        raise ValueError("tile shape is fixed when the plan is created")
+    plan.set_tuning(setting.get("item_units"), setting.get("dense_min"), setting.get("dense_blocks_per_sm"))
+    for k in ("visit_kernel", "interp_kernel", "step_mode", "unit_cap"):
+        if k in setting:
+            setattr(plan, k, setting[k])
+    plan.bin()
