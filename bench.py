@@ -716,10 +716,10 @@ def run_serving(args):
     reqs = serving.poisson_requests(2000.0, n_req, [s.sid for s in specs], seed=2)
     sampler = ClockSampler(local_rank)
     sampler.start()
-    l0 = ibx.kernel_launches()
+    l0 = backend.kernel_launches  # graph replays count the kernels of the captured step
     out = srv.run(reqs)
     torch.cuda.synchronize()
-    launches = ibx.kernel_launches() - l0
+    launches = backend.kernel_launches - l0
     # capacity: the same number of requests all queued at once
     burst = [serving.Request(r.rid, 0.0, r.sid) for r in reqs[: max(1000, n_req // 2)]]
     sat = srv.run(burst)

@@ -85,6 +85,7 @@ class CudaBackend:
         self.kernel = kernel
         self.device = torch.device(device)
         self.graphs = graphs
+        self.kernel_launches = 0  # library kernels run by launch(), graph nodes included
 
     def make_slots(self, n):
         return [self.torch.cuda.Stream(device=self.device) for _ in range(n)]
@@ -103,8 +104,11 @@ class CudaBackend:
         with torch.cuda.stream(slot):
             if sim.graph is not None:
                 sim.graph.replay()
+                self.kernel_launches += sim.kernels_per_step
             else:
+                l0 = ibx.kernel_launches()
                 sim.step(slot)
+                self.kernel_launches += ibx.kernel_launches() - l0
             res = None
             if keep:
                 res = (sim.U.clone(), [t.clone() for t in sim.f])
@@ -141,6 +145,7 @@ class _CudaSim:
         self.plan = ibx.Plan(mk(self.f, self.F), kernel, ibx.MIXED, interp_problems=[mk(self.u, self.U)])
         self.n_markers = spec.n_markers
         self.graph = None
+        self.kernels_per_step = 0  # library kernels in one step (counted at capture)
         # the uploads and fills above ran on the current stream; the steps
         # run on slot streams
         torch.cuda.current_stream().synchronize()
@@ -161,8 +166,10 @@ class _CudaSim:
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
+        l0 = ibx.kernel_launches()
         with torch.cuda.graph(g):
             self.step(torch.cuda.current_stream())
+        self.kernels_per_step = ibx.kernel_launches() - l0
         torch.cuda.synchronize()
         self.graph = g
 

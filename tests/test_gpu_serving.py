@@ -60,13 +60,16 @@ def test_results_alone_equal_results_in_the_mix(serving, oracle):
     assert cases.rel_err(alone[1][0], U_ref) <= MIXED_TOL
     assert cases.rel_err(np.stack(alone[1][1]), f_ref) <= MIXED_TOL
     # the mix: a Poisson stream over all simulations, 4 overlapping slots
-    srv = serving.Server(serving.CudaBackend("IB_4"), 1 << 36, n_slots=4)
+    backend = serving.CudaBackend("IB_4")
+    srv = serving.Server(backend, 1 << 36, n_slots=4)
     for s in specs:
         srv.register(s)
     reqs = serving.poisson_requests(20000.0, 60, [s.sid for s in specs], seed=9)
     out = srv.run(reqs, keep_results=True)
     torch.cuda.synchronize()
     assert out["requests"] == 60
+    # every request replayed its simulation's captured step of library kernels
+    assert backend.kernel_launches == sum(srv.resident[r.sid].kernels_per_step for r in reqs) > 0
     for r in reqs:
         U, f = out["results"][r.rid]
         Ua, fa = alone[r.sid]
