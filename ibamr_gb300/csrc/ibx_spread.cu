@@ -31,6 +31,30 @@ namespace
 constexpr int UNIT_THREADS = 256;  // threads (units) per dense work item
 constexpr int SPARSE_WARPS = 8;    // tiles (warps) per CTA of the visit kernel
 
+// Two FP32 lanes in one 64-bit register: {lo, hi} = {first, second}.
+__device__ __forceinline__ unsigned long long
+pack2(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ void
+unpack2(unsigned long long r, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+
+// d = a * b + c on both FP32 lanes, each rounded once (as fmaf).
+__device__ __forceinline__ unsigned long long
+fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 // Smallest v >= n with v = r (mod m).
 __host__ __device__ constexpr int
 pad_to(int n, int m, int r)
@@ -150,9 +174,20 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                 const int u = D.hucount[t] + k * D.item_units + ul;
                 if (threadIdx.x >= ustep * ncomp * ZS || u >= D.hucount[t + 1]) break;
                 const int2 un = D.home_units[u];
-                float acc[NA];
+                // Even widths accumulate x-pairs with packed FP32x2
+                // multiply-adds (each lane rounded once, as fmaf).
+                constexpr bool PACK = W % 2 == 0;
+                constexpr int WP = W / 2;
+                float acc[PACK ? 1 : NA];
+                unsigned long long accp[PACK ? NA / 2 : 1];
 #pragma unroll
-                for (int i = 0; i < NA; ++i) acc[i] = 0.f;
+                for (int i = 0; i < (PACK ? NA / 2 : NA); ++i)
+                {
+                    if (PACK)
+                        accp[i] = 0ull;
+                    else
+                        acc[i] = 0.f;
+                }
                 int s0[3] = { 0, 0, 0 };
                 if (un.y > 0)
                 {
@@ -205,6 +240,12 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                             if (zh == h) wz = w[2][h * NZ + j2];
                         wzv[j2] = wz * V;
                     }
+                    unsigned long long w0p[PACK ? WP : 1];
+                    if (PACK)
+                    {
+#pragma unroll
+                        for (int q = 0; q < WP; ++q) w0p[q] = pack2(w[0][2 * q], w[0][2 * q + 1]);
+                    }
 #pragma unroll
                     for (int j2 = 0; j2 < NZ; ++j2)
                     {
@@ -212,9 +253,19 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                         for (int i1 = 0; i1 < W; ++i1)
                         {
                             const float wyz = w[1][i1] * wzv[j2];
+                            if (PACK)
+                            {
+                                const unsigned long long aa = pack2(wyz, wyz);
 #pragma unroll
-                            for (int i0 = 0; i0 < W; ++i0)
-                                acc[(j2 * W + i1) * W + i0] = fmaf(w[0][i0], wyz, acc[(j2 * W + i1) * W + i0]);
+                                for (int q = 0; q < WP; ++q)
+                                    accp[(j2 * W + i1) * WP + q] = fma2(w0p[q], aa, accp[(j2 * W + i1) * WP + q]);
+                            }
+                            else
+                            {
+#pragma unroll
+                                for (int i0 = 0; i0 < W; ++i0)
+                                    acc[(j2 * W + i1) * W + i0] = fmaf(w[0][i0], wyz, acc[(j2 * W + i1) * W + i0]);
+                            }
                         }
                     }
                 }
@@ -232,7 +283,15 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
 #pragma unroll
                             for (int i0 = 0; i0 < W; ++i0)
                             {
-                                const float a = acc[(j2 * W + i1) * W + i0];
+                                float a;
+                                if (PACK)
+                                {
+                                    float e0, e1;
+                                    unpack2(accp[(j2 * W + i1) * WP + i0 / 2], e0, e1);
+                                    a = (i0 & 1) ? e1 : e0;
+                                }
+                                else
+                                    a = acc[(j2 * W + i1) * W + i0];
                                 if (a != 0.f) acc2(hi + row + i0, lo + row + i0, a);
                             }
                         }
@@ -654,30 +713,6 @@ struct GatherOccupancy
 {
     static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 3;
 };
-
-// Two FP32 lanes in one 64-bit register: {lo, hi} = {first, second}.
-__device__ __forceinline__ unsigned long long
-pack2(float a, float b)
-{
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-
-__device__ __forceinline__ void
-unpack2(unsigned long long r, float& a, float& b)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-
-// d = a * b + c on both FP32 lanes, each rounded once (as fmaf).
-__device__ __forceinline__ unsigned long long
-fma2(unsigned long long a, unsigned long long b, unsigned long long c)
-{
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 
 template <int DIM, int K, int SH>
 __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::value)
