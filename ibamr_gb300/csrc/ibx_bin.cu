@@ -522,12 +522,13 @@ launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 }
 
 int
-bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s)
+bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s, cudaEvent_t records_done)
 {
     const int nt = D.n_tiles;
     // Counters, cursors and item counts are contiguous: one memset.
     if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
     int rc = launch_bin(dim, kernel, D, s, 0);
+    if (!rc && records_done && cudaEventRecord(records_done, s) != cudaSuccess) rc = IBX_E_CUDA;
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
     if (!rc) rc = launch_bin(dim, kernel, D, s, 1);                 // also counts the work items
     if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 3, scan_tmp, s); // vcount, ucount, items

@@ -7,14 +7,17 @@
 //    home-order markers for one component and keeps the W^d grid values of
 //    the current stencil in registers, so markers of a run (same stencil
 //    base) reuse them and only evaluate their weights and the FP32
-//    multiply-adds.  Every marker (form 0) or the sparse-homed ones (form 1).
+//    multiply-adds.  Every marker in home order (form 0), the sparse-homed
+//    ones (form 1), or every marker in the caller's order (form 2: it needs
+//    only the stencil records, so the step can start it before the counting
+//    sort; fibre markers given in fibre order share runs as in home order).
 //  - interp_units (form 1, dense-homed): the work items of the dense spread
 //    (item_units home units of one tile); one thread per (unit, component)
 //    loads the unit's stencil values once and sums every marker of the unit
 //    from registers.
 // Sum order everywhere: V = sum_z w_z sum_y w_y sum_x w_x u, the separable
-// form of the reference's w(i0,i1,i2) * u (F3D:1309-1328), so both forms
-// give bit-identical results.
+// form of the reference's w(i0,i1,i2) * u (F3D:1309-1328), so every form
+// gives bit-identical results.
 
 #include "ibx_plan.cuh"
 #include "../../include/ibx.h"
@@ -103,14 +106,16 @@ stencil_cells(const PlanProb& P, const Rec& R, int c, int (&co)[3][W])
 // (adjacent threads take the components of one chunk, so that the chunk's
 // records are read from DRAM once).
 template <int DIM, int K>
-__global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D, int select)
+__global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D, int select, int marker_order)
 {
     constexpr int W = KT<K>::W;
     constexpr int NF = DIM == 3 ? W * W * W : W * W;
     constexpr bool CACHE = NF <= 64;
     const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const int c = (int)(tid % D.max_ncomp);
-    const long long total = D.hcount[D.n_tiles];
+    // home order: the binned markers; marker order: every marker (those
+    // without a record, non-finite positions, are skipped)
+    const long long total = marker_order ? D.n_markers : (long long)D.hcount[D.n_tiles];
     const long long m0 = (tid / D.max_ncomp) * CHUNK;
     if (m0 >= total) return;
     const long long m1 = min(m0 + CHUNK, total);
@@ -119,12 +124,13 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D,
     int curp = -1;
     for (long long m = m0; m < m1; ++m)
     {
-        const int g = D.home_list[m];
+        const int g = marker_order ? (int)m : D.home_list[m];
+        if (marker_order && D.home_tile[g] < 0) continue;
         if (select != SEL_ALL && tile_dense(D, D.home_tile[g]) != (select == SEL_DENSE)) continue;
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.marker_offs, D.n_probs, (long long)g);
         const PlanProb& P = D.probs[p];
         if (c >= P.ncomp) continue;
-        const Rec R = D.hrec[m];
+        const Rec R = marker_order ? D.rec[g] : D.hrec[m];
         float w[3][W];
         record_weights<DIM, K>(P, R, c, w);
         const float* q = static_cast<const float*>(P.qi[c]);
@@ -246,7 +252,7 @@ launch_interp_k(const DevPlan& D, cudaStream_t s)
     const long long chunks = (D.n_markers + CHUNK - 1) / CHUNK;
     const unsigned bx = (unsigned)((chunks * D.max_ncomp + INTERP_THREADS - 1) / INTERP_THREADS);
     if (bx == 0) return IBX_OK;
-    interp_chunks<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D, units ? SEL_SPARSE : SEL_ALL);
+    interp_chunks<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D, units ? SEL_SPARSE : SEL_ALL, D.interp_form == 2);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }

@@ -345,16 +345,21 @@ ibx_plan_step(ibx_plan* plan, void* stream)
     using namespace ibx;
     if (!plan) return IBX_E_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s);
+    // Interpolation in marker order needs only the stencil records: in the
+    // concurrent mode it forks as soon as they exist, beside the counting
+    // sort; the other forms fork after the whole binning.
+    const bool early = plan->step_mode == 1 && plan->D.interp_form == 2;
+    int rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr);
     if (rc) return rc;
     if (plan->step_mode == 0)
     {
         rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
         return rc ? rc : launch_interp(plan->dim, plan->kernel, plan->D, s);
     }
-    // spread (stream) and interpolation (side) read the same bins and write
-    // different arrays: they overlap on the device
-    if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
+    // spread (stream) and interpolation (side) read the same records and
+    // write different arrays: they overlap on the device
+    if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
+        cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
         return IBX_E_CUDA;
     rc = launch_interp(plan->dim, plan->kernel, plan->D, plan->side);
     const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
@@ -480,7 +485,7 @@ ibx_plan_get_step_mode(const ibx_plan* plan)
 int
 ibx_plan_set_interp_kernel(ibx_plan* plan, int form)
 {
-    if (!plan || form < 0 || form > 1) return IBX_E_ARG;
+    if (!plan || form < 0 || form > 2) return IBX_E_ARG;
     plan->D.interp_form = form;
     return IBX_OK;
 }

@@ -149,7 +149,7 @@ struct DevPlan
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
     int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component)
-    int interp_form;  // 1: dense-homed markers interpolated per home unit, 0: all in chunks
+    int interp_form;  // 0: chunks in home order; 1: dense-homed per home unit; 2: chunks in marker order
     int unit_cap;     // most markers per home unit (1..32)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
@@ -192,7 +192,10 @@ bool fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx);
 
 // The binning sequence of one step (counters zeroed, bin, scans, scatters,
 // dense work items).
-int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s);
+// Binning of a plan on stream s; records_done (optional) is recorded once the
+// stencil records and home tiles exist (before the counting sort).
+int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s,
+                 cudaEvent_t records_done = nullptr);
 
 template <typename T>
 __device__ __forceinline__ int

@@ -273,11 +273,13 @@ int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, i
 int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_visit_kernel(const ibx_plan* plan);
 /* Form of the interpolation (no reference counterpart; chosen by the
- * autotuner): 1 = markers of dense home tiles interpolated per home unit
- * (the unit's stencil values loaded once, every marker of the unit summed
- * from them), the others in chunks of consecutive markers; 0 = every marker
- * in chunks (default).  Both forms sum in the same order: identical
- * results. */
+ * autotuner): 0 = every marker in chunks of consecutive home-order markers
+ * (default); 1 = markers of dense home tiles interpolated per home unit (the
+ * unit's stencil values loaded once, every marker of the unit summed from
+ * them), the others in chunks; 2 = every marker in chunks in the caller's
+ * marker order, which needs only the stencil records, so that
+ * ibx_plan_step (concurrent mode) starts it beside the counting sort.  Every
+ * form sums in the same order: identical results. */
 int ibx_plan_set_interp_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_interp_kernel(const ibx_plan* plan);
 /* How ibx_plan_step orders spread and interpolation after the binning (no

@@ -360,9 +360,12 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim):
-    """ibx_plan_step (spread and interpolation on two streams) gives the
-    oracle's answer like the separate calls."""
+@pytest.mark.parametrize("step_mode", [0, 1])
+@pytest.mark.parametrize("interp_form", [0, 1, 2])
+def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_form, step_mode):
+    """ibx_plan_step (spread and interpolation on two streams, or one after
+    the other; the marker-order interpolation forked before the counting
+    sort) gives the oracle's answer, step after step."""
     rng = np.random.default_rng(61 + dim)
     N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
     n = 2500
@@ -378,11 +381,17 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim):
     mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
                                        [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
     plan = ibx.Plan(mk(f_t, F_t), "IB_4", ibx.MIXED, interp_problems=[mk(u_t, U_t)])
-    plan.step()
-    torch.cuda.synchronize()
-    f = np.stack([t.double().cpu().numpy() for t in f_t])
-    assert cases.rel_err(f, f_ref) <= MIXED_TOL
-    assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
+    plan.interp_kernel = interp_form
+    plan.step_mode = step_mode
+    for _ in range(2):
+        for t in f_t:
+            t.zero_()
+        U_t.zero_()
+        plan.step()
+        torch.cuda.synchronize()
+        f = np.stack([t.double().cpu().numpy() for t in f_t])
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL
+        assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
     assert plan.status() == ibx.OK
     plan.close()
 
@@ -419,9 +428,10 @@ def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_sha
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
 @pytest.mark.parametrize("dense_min", [0, 8])
 def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, tile_shape, dense_min):
-    """Both interpolation forms (dense-homed markers per home unit or in
-    chunks) sum in the same order: bit-identical results (every tile dense,
-    then a mix), both within the bar of the oracle."""
+    """Every interpolation form (chunks in home order, dense-homed markers per
+    home unit, chunks in marker order) sums in the same order: bit-identical
+    results (every tile dense, then a mix), all within the bar of the
+    oracle."""
     rng = np.random.default_rng(91 + N[0] + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     n = 2000
     X = seam_markers(rng, n, dim)
@@ -430,7 +440,7 @@ def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, t
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
     got = []
-    for form in (1, 0):
+    for form in (1, 2, 0):
         f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min,
                                 tile_shape=tile_shape, interp_kernel=form)
         assert pi.interp_kernel == form
