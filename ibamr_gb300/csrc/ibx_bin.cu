@@ -283,8 +283,8 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
     agg_count(D.hucount, ht, lead);
 }
 
-// Places a unit group: its leader reserves a contiguous range of the list
-// and one unit record; returns the lane's slot in the list.
+// Places a home unit group: its leader reserves a contiguous range of the
+// list and one unit record; returns the lane's slot in the list.
 __device__ __forceinline__ int
 place_group(unsigned grp, int tile, int* cursor, const int* start, int* ucursor, const int* ustart, int2* units)
 {
@@ -348,16 +348,7 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
-        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
-        const unsigned act = __ballot_sync(0xffffffffu, v);
-        bool lead = false;
-        if (v)
-        {
-            const unsigned grp = unit_group(act, t, key);
-            lead = (threadIdx.x & 31) == __ffs(grp) - 1;
-        }
-        agg_count(D.vcount, t, v);
-        agg_count(D.ucount, t, lead);
+        agg_count(D.vcount, v ? visit_tile_id<DIM>(P, tl, nt, k) : 0, v);
     }
 }
 
@@ -372,13 +363,7 @@ __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
     const int p = (!valid || D.n_probs == 1) ? 0 : find_in_offsets(D.marker_offs, D.n_probs, g);
     const PlanProb& P = D.probs[p];
     int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
-    unsigned long long key = 0;
-    if (valid)
-    {
-        const Rec R = D.rec[g];
-        nvis = visit_tiles<DIM, K, SH>(P, R, tl, nt);
-        key = base_key(R);
-    }
+    if (valid) nvis = visit_tiles<DIM, K, SH>(P, D.rec[g], tl, nt);
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
@@ -386,8 +371,13 @@ __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
         const unsigned act = __ballot_sync(0xffffffffu, v);
         if (v)
         {
-            const unsigned grp = unit_group(act, t, key);
-            const int pos = place_group(grp, t, D.vcursor, D.vcount, D.ucursor, D.ucount, D.units);
+            // lanes visiting the same tile share one reservation
+            const unsigned grp = __match_any_sync(act, t);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(grp) - 1;
+            int base = 0;
+            if (lane == leader) base = D.vcount[t] + atomicAdd(&D.vcursor[t], __popc(grp));
+            const int pos = __shfl_sync(grp, base, leader) + __popc(grp & ((1u << lane) - 1));
             if (pos < D.n_visit_cap)
                 D.visit_list[pos] = (int)g;
             else
@@ -531,7 +521,7 @@ bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t 
     if (!rc && records_done && cudaEventRecord(records_done, s) != cudaSuccess) rc = IBX_E_CUDA;
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
     if (!rc) rc = launch_bin(dim, kernel, D, s, 1);                 // also counts the work items
-    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 3, scan_tmp, s); // vcount, ucount, items
+    if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 2, scan_tmp, s); // vcount, items
     if (!rc) rc = launch_bin(dim, kernel, D, s, 2);
     if (!rc) rc = launch_items_fill(D, s);
     return rc;

@@ -95,7 +95,6 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     const size_t o_home_list = take(sizeof(int) * nm);
     const size_t o_visit = take(sizeof(int) * z.visit_cap);
     const size_t o_home_units = take(sizeof(int2) * nm);
-    const size_t o_units = take(sizeof(int2) * z.visit_cap);
     c.o_status = take(sizeof(int) * 4);
     const size_t o_scan = take(sizeof(int) * SCAN_TMP_INTS);
     c.bytes = off;
@@ -115,17 +114,14 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.hcount = counts;
     D.hucount = counts + (nt + 1);
     D.vcount = counts + 2 * (nt + 1);
-    D.ucount = counts + 3 * (nt + 1);
-    D.items = counts + 4 * (nt + 1);
-    D.hcursor = counts + 5 * (nt + 1);
+    D.items = counts + 3 * (nt + 1);
+    D.hcursor = counts + 4 * (nt + 1);
     D.hucursor = D.hcursor + nt;
     D.vcursor = D.hucursor + nt;
-    D.ucursor = D.vcursor + nt;
     D.home_list = reinterpret_cast<int*>(b + o_home_list);
     D.visit_list = reinterpret_cast<int*>(b + o_visit);
     D.n_visit_cap = z.visit_cap;
     D.home_units = reinterpret_cast<int2*>(b + o_home_units);
-    D.units = reinterpret_cast<int2*>(b + o_units);
     D.item_tile = reinterpret_cast<int*>(b + o_item_tile);
     D.n_item_cap = (int)z.item_cap;
     D.item_units = ITEM_UNITS;

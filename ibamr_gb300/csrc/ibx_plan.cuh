@@ -123,24 +123,21 @@ struct DevPlan
     Rec* hrec;        // [n_markers], home-tile order (same order as home_list)
     int* home_tile;   // [n_markers]
     // Counters (zeroed together each step; the *count arrays are scanned in
-    // place into start offsets; hcount/hucount, then vcount/ucount/items,
-    // are adjacent so that each group is scanned by one launch).
+    // place into start offsets; hcount/hucount and vcount/items are
+    // adjacent so that each pair is scanned by one launch).
     int* hcount;      // [n_tiles+1] markers per home tile
     int* hucount;     // [n_tiles+1] home units per tile
     int* vcount;      // [n_tiles+1] visits per tile (sparse-homed markers only)
-    int* ucount;      // [n_tiles+1] visit units per tile
+    int* items;       // [n_tiles+1] dense-tile spread work items, scanned into offsets
     int* hcursor;     // [n_tiles]
     int* hucursor;    // [n_tiles]
     int* vcursor;     // [n_tiles]
-    int* ucursor;     // [n_tiles]
-    int* items;       // [n_tiles+1] dense-tile spread work items, scanned into offsets
     int* home_list;   // [n_markers] global marker ids grouped by home tile
     int* visit_list;  // [n_visit_cap] global marker ids grouped by visited tile
     long long n_visit_cap;
-    // A unit is a run of consecutive list entries that share the tile and
-    // every stencil base: (start in the list, length).
+    // A home unit is a run of consecutive home-list entries that share the
+    // tile and every stencil base: (start in the list, length).
     int2* home_units; // [n_markers]
-    int2* units;      // [n_visit_cap]
     int* item_tile;   // [n_item_cap] tile of each work item
     int n_item_cap;
     int item_units;   // home units per dense work item (one per thread, <= 256)
@@ -148,23 +145,24 @@ struct DevPlan
     int dense_blocks_per_sm; // CTAs per SM of the dense spread grid
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
-    int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component)
+    int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component); 2: tile gathered
     int interp_form;  // 0: chunks in home order; 1: dense-homed per home unit; 2: chunks in marker order
     int unit_cap;     // most markers per home unit (1..32)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
 };
 
-// Block sums of the exclusive scans: up to 3 arrays of up to 2048 blocks.
-constexpr int SCAN_TMP_INTS = 3 * 2048;
+// Block sums of the exclusive scans: up to 2 arrays of up to 2048 blocks.
+constexpr int SCAN_TMP_INTS = 2 * 2048;
 
 // Number of ints of the counter block starting at hcount: hcount, hucount,
-// vcount, ucount and items ([n_tiles + 1] each, adjacent so that they scan
-// together), then the four cursors ([n_tiles] each).
+// vcount and items ([n_tiles + 1] each; the pairs hcount/hucount and
+// vcount/items are adjacent so that each pair scans in one launch), then the
+// three cursors ([n_tiles] each).
 __host__ __device__ inline size_t
 counter_ints(int n_tiles)
 {
-    return 9 * (size_t)n_tiles + 5;
+    return 7 * (size_t)n_tiles + 4;
 }
 
 // Buffer layout of a plan for the given sizes; with base == nullptr only the

@@ -28,8 +28,8 @@ from . import ibx
 # ---------------------------------------------------------------------------
 def plan_bytes_estimate(dim, N, n_markers):
     """Upper bound of ibx_plan_scratch_bytes for one periodic problem: the
-    buffers of the plan (records in two orders, lists, units, counters, work
-    items), with the visit capacity the library reserves."""
+    buffers of the plan (records in two orders, lists, home units, counters,
+    work items), with the visit capacity the library reserves."""
     E = 8 if dim == 3 else 16
     tiles = int(np.prod([(n + E - 1) // E for n in N]))
     per = 1
@@ -40,10 +40,10 @@ def plan_bytes_estimate(dim, N, n_markers):
     b = 0
     b += 2 * 32 * n_markers                     # records (marker order, home order)
     b += 3 * 4 * n_markers + 8 * n_markers      # home tile, home list, home units
-    b += visit_cap * (4 + 8)                    # visit list, visit units
-    b += 4 * (9 * tiles + 5)                    # counters
+    b += visit_cap * 4                          # visit list
+    b += 4 * (7 * tiles + 4)                    # counters
     b += 4 * (tiles + n_markers // 10 + 1)      # dense work items
-    b += 4 * 3 * 2048 + 4096 + 14 * 256         # scan scratch, descriptors, alignment
+    b += 4 * 2 * 2048 + 4096 + 13 * 256         # scan scratch, descriptors, alignment
     return b
 
 
