@@ -40,8 +40,16 @@ METRIC = "spread+interp markers/s"
 UNIT = "markers/s"
 KERNEL = "IB_4"
 KERNEL_W = 4
+KERNEL_WIDTHS = {"IB_3": 3, "IB_4": 4, "IB_6": 6, "PIECEWISE_CUBIC": 4, "BSPLINE_4": 4, "PIECEWISE_LINEAR": 2}
 N_GRID = 256
 WORKLOAD = "helices64x25k+uniform400k_256cube_IB4"
+
+
+def use_kernel(name):
+    """Select the delta kernel of the helices workload (names its workload)."""
+    global KERNEL, KERNEL_W, WORKLOAD
+    KERNEL, KERNEL_W = name, KERNEL_WIDTHS[name]
+    WORKLOAD = "helices64x25k+uniform400k_256cube_" + name.replace("_", "")
 
 
 def parse_args():
@@ -54,6 +62,9 @@ def parse_args():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--setting", default=None,
                     help="fixed plan setting k=v,... as printed under tuning.setting (skips the autotuner)")
+    ap.add_argument("--kernel", default="IB_4", choices=sorted(KERNEL_WIDTHS),
+                    help="delta kernel of the helices workload (the metric is quoted on IB_4; the same "
+                         "configuration also runs IB_6)")
     ap.add_argument("--workload", default="helices", choices=["helices", "batched", "serving"],
                     help="helices: 2M markers on 256^3 (default); batched: 512 independent 2D problems in one "
                          "CUDA graph; serving: Poisson request stream over resident simulations")
@@ -782,6 +793,10 @@ def run_serving(args):
 
 def main():
     args = parse_args()
+    if args.kernel != "IB_4":
+        if args.workload != "helices":
+            raise SystemExit("--kernel applies to the helices workload")
+        use_kernel(args.kernel)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

@@ -148,6 +148,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     const PlanCarve c = carve_plan(z, b, D);
     D.zsplit = dense_zsplit(dim, kernel_width(kernel));
     D.item_units = 2 * (256 / (ncomp * D.zsplit)) < 256 ? 2 * (256 / (ncomp * D.zsplit)) : 256;
+    if (D.item_units < 32) D.item_units = 32; // at least the units per item the capacity assumes
     D.max_ncomp = ncomp;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const long long moffs[2] = { 0, nm };

@@ -320,7 +320,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     }
     D.zsplit = dense_zsplit(dim, kernel_width(kernel));
     // two units per thread: the region is zeroed and flushed once per item
-    D.item_units = std::min(ITEM_UNITS, 2 * (ITEM_UNITS / (max_ncomp * D.zsplit)));
+    D.item_units = std::max(MIN_ITEM_UNITS, std::min(ITEM_UNITS, 2 * (ITEM_UNITS / (max_ncomp * D.zsplit))));
     D.max_ncomp = max_ncomp;
     plan->dmem = dmem;
     plan->dbytes = c.bytes;

@@ -28,11 +28,12 @@ struct TileT
 
 // Threads per (unit, component) of the dense-tile spread: a 4 x 4 x 4
 // footprint is split into two z-halves held by adjacent threads (32
-// accumulators each), other footprints are held by one thread.
+// accumulators each), a 6 x 6 x 6 one into six z-planes (36 each), other
+// footprints are held by one thread.
 __host__ __device__ constexpr int
 dense_zsplit(int dim, int width)
 {
-    return (dim == 3 && width == 4) ? 2 : 1;
+    return dim == 3 && width == 4 ? 2 : dim == 3 && width == 6 ? 6 : 1;
 }
 
 // Stencil width of a kernel id (host side).

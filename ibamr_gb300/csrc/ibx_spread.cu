@@ -76,12 +76,12 @@ struct Region
     static constexpr int R2 = DIM == 3 ? T::E2 + W : 1;
     static constexpr int RP = R0 * R1 * R2;
     static constexpr int NF = DIM == 3 ? W * W * W : W * W;
-    // Footprints up to 4^3 points are accumulated in registers per unit,
-    // split over ZS threads along z.
-    static constexpr bool regs = NF <= 64;
+    // A unit's footprint is accumulated in registers, split over ZS threads
+    // along z, when a thread's share is at most 64 points (every kernel).
     static constexpr int ZS = dense_zsplit(DIM, W);
     static constexpr int NZ = (DIM == 3 ? W : 1) / ZS; // z-planes per thread
     static constexpr int NA = NZ * W * W;              // accumulators per thread
+    static constexpr bool regs = NA <= 64;
     // Padded shared-memory layout: x + R0*y + PSR*z within a component;
     // the threads of one unit (its components and z-halves) start 4 banks
     // apart per z-half (with NZ = 2: PSR = 2 mod 32) and 8 banks apart per
