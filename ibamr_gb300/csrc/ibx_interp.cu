@@ -12,9 +12,10 @@
 //    only the stencil records, so the step can start it before the counting
 //    sort; fibre markers given in fibre order share runs as in home order).
 //  - interp_units (form 1, dense-homed): the work items of the dense spread
-//    (item_units home units of one tile); one thread per (unit, component)
-//    loads the unit's stencil values once and sums every marker of the unit
-//    from registers.
+//    (item_units home units of one tile); a group of lanes per (unit,
+//    component), the footprint's z-planes split over the group, loads the
+//    unit's stencil values once and sums every marker of the unit from
+//    registers.
 // Sum order everywhere: V = sum_z w_z sum_y w_y sum_x w_x u, the separable
 // form of the reference's w(i0,i1,i2) * u (F3D:1309-1328), so every form
 // gives bit-identical results.
@@ -173,15 +174,37 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D,
     }
 }
 
-// Dense-homed markers by home unit: one thread per (unit, component) of a
-// dense work item loads the unit's W^d grid values once into registers and
-// sums every marker of the unit from them.  Footprints of at most 64 points.
+// Lanes per (home unit, component) of interp_units: the footprint's z-planes
+// are split over ZS adjacent lanes (dense_zsplit, as for the dense spread),
+// each caching NZ planes of W x W values.
+template <int DIM, int W>
+struct UnitSplit
+{
+    static constexpr int ZS = dense_zsplit(DIM, W);
+    static constexpr int NZ = (DIM == 3 ? W : 1) / ZS;
+    static constexpr int NC = NZ * W * W; // cached values per lane
+    static constexpr int GPW = 32 / ZS;   // lane groups per warp
+};
+
+// Dense-homed markers by home unit: a group of ZS lanes per (unit,
+// component) of a dense work item loads the unit's W^d grid values once
+// (NZ planes per lane) and sums every marker of the unit from registers.
+// Each lane forms sum_y w_y sum_x w_x u for its planes; the first lane of
+// the group gathers the plane sums with shuffles and adds them in z order,
+// so the sum order is the chunked form's.
 template <int DIM, int K>
 __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
-    constexpr int NF = DIM == 3 ? W * W * W : W * W;
-    if (NF > 64) return; // wider footprints are interpolated in chunks
+    using US = UnitSplit<DIM, W>;
+    constexpr int ZS = US::ZS, NZ = US::NZ, NC = US::NC;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane >= US::GPW * ZS) return;
+    const int zh = lane % ZS;                       // this lane's planes: zh * NZ ...
+    const int lead = lane - zh;                     // first lane of the group
+    const unsigned gmask = ((1u << ZS) - 1u) << lead; // the group's lanes
+    const int group = warp * US::GPW + lane / ZS;
+    const int n_groups = (INTERP_THREADS / 32) * US::GPW;
     const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
     for (int item = blockIdx.x; item < n_items; item += gridDim.x)
     {
@@ -190,38 +213,63 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
         const PlanProb& P = D.probs[p];
         const int ncomp = P.ncomp;
-        const int c = threadIdx.x % ncomp;
-        const int ustep = blockDim.x / ncomp;
-        if ((int)threadIdx.x >= ustep * ncomp) continue;
-        const float* q = static_cast<const float*>(P.qi[c]);
+        const int u0 = D.hucount[t] + k * D.item_units;
+        const int nu = min(D.item_units, D.hucount[t + 1] - u0);
         float* Qi = static_cast<float*>(P.Qi);
         const long long n0 = P.N[0], n01 = (long long)P.N[0] * P.N[1];
-        for (int ul = threadIdx.x / ncomp; ul < D.item_units; ul += ustep)
+        for (int pair = group; pair < nu * ncomp; pair += n_groups)
         {
-            const int u = D.hucount[t] + k * D.item_units + ul;
-            if (u >= D.hucount[t + 1]) break;
-            const int2 un = D.home_units[u];
+            const int c = pair % ncomp;
+            const int2 un = D.home_units[u0 + pair / ncomp];
             if (un.y <= 0) continue;
-            float uv[NF > 64 ? 1 : NF];
+            const float* q = static_cast<const float*>(P.qi[c]);
+            float uv[NC];
             {
                 int co[3][W];
                 stencil_cells<DIM, W>(P, D.hrec[un.x], c, co);
 #pragma unroll
-                for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
+                for (int j2 = 0; j2 < NZ; ++j2)
+                {
+                    // plane zh * NZ + j2, selected without dynamic indexing
+                    int cz = co[2][j2];
+#pragma unroll
+                    for (int h = 1; h < ZS; ++h)
+                        if (zh == h) cz = co[2][h * NZ + j2];
 #pragma unroll
                     for (int i1 = 0; i1 < W; ++i1)
 #pragma unroll
                         for (int i0 = 0; i0 < W; ++i0)
-                            uv[(i2 * W + i1) * W + i0] =
-                                __ldg(q + (DIM == 3 ? co[2][i2] * n01 : 0) + co[1][i1] * n0 + co[0][i0]);
+                            uv[(j2 * W + i1) * W + i0] =
+                                __ldg(q + (DIM == 3 ? cz * n01 : 0) + co[1][i1] * n0 + co[0][i0]);
+                }
             }
             for (int v = un.x; v < un.x + un.y; ++v)
             {
                 float w[3][W];
                 record_weights<DIM, K>(P, D.hrec[v], c, w);
-                const float V =
-                    separable_sum<DIM, W>(w, [&](int i0, int i1, int i2) { return uv[(i2 * W + i1) * W + i0]; });
-                Qi[(long long)P.Q_depth * (D.home_list[v] - P.marker0) + c] = V;
+                float vy[NZ];
+#pragma unroll
+                for (int j2 = 0; j2 < NZ; ++j2)
+                {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int i1 = 0; i1 < W; ++i1)
+                    {
+                        float vx = 0.f;
+#pragma unroll
+                        for (int i0 = 0; i0 < W; ++i0) vx = fmaf(w[0][i0], uv[(j2 * W + i1) * W + i0], vx);
+                        acc = fmaf(w[1][i1], vx, acc);
+                    }
+                    vy[j2] = acc;
+                }
+                float V = 0.f;
+#pragma unroll
+                for (int z = 0; z < (DIM == 3 ? W : 1); ++z)
+                {
+                    const float vz = ZS == 1 ? vy[z % NZ] : __shfl_sync(gmask, vy[z % NZ], lead + z / NZ);
+                    V = fmaf(DIM == 3 ? w[2][z] : 1.f, vz, V);
+                }
+                if (zh == 0) Qi[(long long)P.Q_depth * (D.home_list[v] - P.marker0) + c] = V;
             }
         }
     }
@@ -232,8 +280,7 @@ int
 launch_interp_k(const DevPlan& D, cudaStream_t s)
 {
     constexpr int W = KT<K>::W;
-    constexpr int NF = DIM == 3 ? W * W * W : W * W;
-    const bool units = D.interp_form == 1 && NF <= 64;
+    const bool units = D.interp_form == 1 && UnitSplit<DIM, W>::NC <= 64;
     if (units)
     {
         int dev = 0, sms = 152, per_sm = 0;
