@@ -448,9 +448,62 @@ __global__ void items_fill(const DevPlan D)
 }
 } // namespace
 
+// Exclusive scan of array blockIdx.x (n ints, arrays n apart) by one CTA:
+// each thread sums a contiguous segment of at most SINGLE_PER values, the
+// segment totals are scanned across the block with warp shuffles, and each
+// thread rewrites its segment.  One launch for up to 1024 * SINGLE_PER values
+// (beyond that the three-launch scan is faster: the single CTA's serial
+// segments are latency-bound).
+constexpr int SINGLE_PER = 8;
+
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_single(int* data, int n)
+{
+    __shared__ int warp_tot[SCAN_BLOCK / 32];
+    int* a = data + (long long)blockIdx.x * n;
+    const int per = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    const int b = min((int)threadIdx.x * per, n), e = min(b + per, n);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += a[i];
+    int x = sum; // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        int t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    int run = x - sum + (warp ? warp_tot[warp - 1] : 0);
+    for (int i = b; i < e; ++i)
+    {
+        const int v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
 int
 exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s)
 {
+    if (n <= SCAN_BLOCK * SINGLE_PER)
+    {
+        scan_single<<<count, SCAN_BLOCK, 0, s>>>(data, n);
+        note_launches(1);
+        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+    }
     const int nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
     if (nb > SCAN_ITEMS || (long long)nb * count > SCAN_TMP_INTS) return IBX_E_TOO_LARGE; // more than 4M entries
     scan_blocks<<<dim3(nb, count), SCAN_BLOCK, 0, s>>>(data, n, tmp, nb);

@@ -484,3 +484,35 @@ def test_unit_cap(ibx, oracle, kernel, dim, cap):
     assert cases.rel_err(f, f_ref) <= MIXED_TOL
     assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
     plan.close()
+
+
+@pytest.mark.parametrize("N", [[256, 250], [4128, 4096]])
+def test_counting_sort_scans_small_and_large_tile_counts(ibx, N):
+    """The counting sort's scans: one CTA up to 8,192 tile counters, three
+    launches above (4128 x 4096 cells = 66,048 tiles of 16 x 16); tile
+    starts are the exclusive scan of the home-tile counts, bit-exact, and
+    the spread matches the per-marker plain form's mass."""
+    rng = np.random.default_rng(404 + N[0])
+    dim, n = 2, 60000
+    X = rng.uniform(0.0, 1.0, size=n * dim)
+    X_t = torch.tensor(X, device="cuda")
+    f_t = [torch.zeros(N[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    F_t = torch.ones(n * dim, dtype=torch.float32, device="cuda")
+    prob = ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0, 0], [N[0] - 1, N[1] - 1], [1.0 / N[0], 1.0 / N[1]],
+                            [0.0, 0.0], [1.0, 1.0], f_t, X_t, F_t)
+    plan = ibx.Plan(prob, "IB_4", ibx.MIXED)
+    plan.set_tuning(dense_min=4)
+    plan.bin()
+    plan.spread()
+    torch.cuda.synchronize()
+    bc, bs, ht, ts, hl = plan.bins(n)
+    counts = np.bincount(ht, minlength=plan.n_tiles)
+    assert plan.n_tiles == ((N[0] + 15) // 16) * ((N[1] + 15) // 16)
+    assert ts[0] == 0 and np.array_equal(np.diff(ts), counts)
+    assert np.array_equal(np.sort(hl), np.arange(n))
+    # unit forces: every component's grid sum is n / (dx dy) (weights sum to 1)
+    for a in range(dim):
+        total = float(f_t[a].double().sum()) / (N[0] * N[1])
+        assert abs(total - n) <= 1e-4 * n
+    assert plan.status() == ibx.OK
+    plan.close()
