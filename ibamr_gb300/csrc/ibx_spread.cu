@@ -29,6 +29,7 @@ namespace ibx
 namespace
 {
 constexpr int UNIT_THREADS = 256;  // threads (units) per dense work item
+constexpr int MAX_ITEM_UNITS = 256; // largest item_units ibx_plan_set_tuning accepts
 constexpr int SPARSE_WARPS = 8;    // tiles (warps) per CTA of the visit kernel
 
 // Two FP32 lanes in one 64-bit register: {lo, hi} = {first, second}.
@@ -157,6 +158,34 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
         for (int i = threadIdx.x; i < ncomp * CSTR / 4; i += blockDim.x)
             reinterpret_cast<float4*>(sm)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int i = ncomp * CSTR / 4 * 4 + threadIdx.x; i < ncomp * CSTR; i += blockDim.x) sm[i] = 0.f;
+        // The item's units, longest first (a counting sort by length in
+        // shared memory), so that the threads of a warp take units of
+        // similar length and finish together.
+        __shared__ int s_order[MAX_ITEM_UNITS];
+        __shared__ int s_start[33];
+        const int u0 = D.hucount[t] + k * D.item_units;
+        const int nu = max(0, min(D.item_units, D.hucount[t + 1] - u0));
+        if (RG::regs)
+        {
+            if (threadIdx.x < 33) s_start[threadIdx.x] = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < nu; i += blockDim.x)
+                atomicAdd(&s_start[32 - min(D.home_units[u0 + i].y, 32)], 1);
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                int run = 0;
+                for (int b = 0; b < 33; ++b)
+                {
+                    const int v = s_start[b];
+                    s_start[b] = run;
+                    run += v;
+                }
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < nu; i += blockDim.x)
+                s_order[atomicAdd(&s_start[32 - min(D.home_units[u0 + i].y, 32)], 1)] = i;
+        }
         __syncthreads();
         const float* Qf = static_cast<const float*>(P.Q);
         if (RG::regs)
@@ -169,10 +198,10 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
             const int c = threadIdx.x % ncomp;
             const int zh = (threadIdx.x / ncomp) % ZS;
             const int ustep = blockDim.x / (ncomp * ZS);
-            for (int ul = threadIdx.x / (ncomp * ZS); ul < D.item_units; ul += ustep)
+            for (int ul = threadIdx.x / (ncomp * ZS); ul < nu; ul += ustep)
             {
-                const int u = D.hucount[t] + k * D.item_units + ul;
-                if (threadIdx.x >= ustep * ncomp * ZS || u >= D.hucount[t + 1]) break;
+                if (threadIdx.x >= ustep * ncomp * ZS) break;
+                const int u = u0 + s_order[ul];
                 const int2 un = D.home_units[u];
                 // Even widths accumulate x-pairs with packed FP32x2
                 // multiply-adds (each lane rounded once, as fmaf).
