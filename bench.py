@@ -288,7 +288,7 @@ def run_ours(args):
     elif args.no_tune:
         plan = make_plan(0)
     else:
-        plan, tuned = tuning.autotune_shape(make_plan)
+        plan, tuned = tuning.autotune_shape(make_plan, reps=8)
     setting = tuning.setting_string(tuning.setting_of(plan))
 
     def step():
@@ -534,7 +534,7 @@ def run_batched(args):
     if args.setting:
         B.configure(tuning.parse_setting(args.setting))
     elif not args.no_tune:
-        B.autotune()  # on the benchmark's own forces and velocities
+        B.autotune(reps=8)  # on the benchmark's own forces and velocities
     setting = tuning.setting_string(tuning.setting_of(B.plan))
     stream = torch.cuda.current_stream()
 

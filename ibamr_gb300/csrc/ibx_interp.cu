@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
     using US = UnitSplit<DIM, W>;
     constexpr int ZS = US::ZS, NZ = US::NZ, NC = US::NC;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane >= US::GPW * ZS) return;
+    const bool active = lane < US::GPW * ZS;       // lanes beyond the last full group idle
     const int zh = lane % ZS;                       // this lane's planes: zh * NZ ...
     const int lead = lane - zh;                     // first lane of the group
     const unsigned gmask = ((1u << ZS) - 1u) << lead; // the group's lanes
@@ -214,13 +214,37 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
         const PlanProb& P = D.probs[p];
         const int ncomp = P.ncomp;
         const int u0 = D.hucount[t] + k * D.item_units;
-        const int nu = min(D.item_units, D.hucount[t + 1] - u0);
+        const int nu = max(0, min(D.item_units, D.hucount[t + 1] - u0));
         float* Qi = static_cast<float*>(P.Qi);
         const long long n0 = P.N[0], n01 = (long long)P.N[0] * P.N[1];
+        // the item's units, longest first, as in the dense spread
+        __shared__ int s_order[256];
+        __shared__ int s_start[33];
+        __syncthreads(); // the previous item's readers of s_order are done
+        if (threadIdx.x < 33) s_start[threadIdx.x] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nu; i += blockDim.x)
+            atomicAdd(&s_start[32 - min(D.home_units[u0 + i].y, 32)], 1);
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            int run = 0;
+            for (int b = 0; b < 33; ++b)
+            {
+                const int v = s_start[b];
+                s_start[b] = run;
+                run += v;
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nu; i += blockDim.x)
+            s_order[atomicAdd(&s_start[32 - min(D.home_units[u0 + i].y, 32)], 1)] = i;
+        __syncthreads();
+        if (!active) continue;
         for (int pair = group; pair < nu * ncomp; pair += n_groups)
         {
             const int c = pair % ncomp;
-            const int2 un = D.home_units[u0 + pair / ncomp];
+            const int2 un = D.home_units[u0 + s_order[pair / ncomp]];
             if (un.y <= 0) continue;
             const float* q = static_cast<const float*>(P.qi[c]);
             float uv[NC];
