@@ -143,7 +143,7 @@ tiles_1d(int b, int span, int N, int E, int* out)
     int n = 0;
     for (int i = 0; i < span; ++i)
     {
-        const int tile = wrap_cell(b + i, N) / E;
+        const int tile = wrap_from_base(b + i, N) / E;
         bool seen = false;
         for (int k = 0; k < n; ++k) seen = seen || out[k] == tile;
         if (!seen && n < 4) out[n++] = tile;
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
             finite = finite && (bs - bc == 0 || bs - bc == 1);
             R.rc[d] = rc;
             R.rs[d] = rs;
-            home[d] = wrap_cell(bc + (W - 1) / 2, N) / TileT<DIM, SH>::edge(d);
+            home[d] = wrap_from_base(bc + (W - 1) / 2, N) / TileT<DIM, SH>::edge(d);
         }
         R.key = rkey;
         if (!finite)

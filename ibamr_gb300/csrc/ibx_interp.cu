@@ -99,7 +99,7 @@ stencil_cells(const PlanProb& P, const Rec& R, int c, int (&co)[3][W])
         }
         const int b = (P.side && d == c) ? R.bs(d) : R.bc(d);
 #pragma unroll
-        for (int i = 0; i < W; ++i) co[d][i] = wrap_cell(b + i, P.N[d]);
+        for (int i = 0; i < W; ++i) co[d][i] = wrap_from_base(b + i, P.N[d]);
     }
 }
 

@@ -231,6 +231,16 @@ tile_origin(const PlanProb& P, int lt, int* org)
     org[2] = DIM == 3 ? (lt / (P.ntile[0] * P.ntile[1])) * T::E2 : 0;
 }
 
+// Cell x = b + i of a stencil whose base b lies in [0, N] (the bases of a
+// plan's records), wrapped into [0, N): one conditional subtraction unless
+// the grid is narrower than the stencil.
+__device__ __forceinline__ int
+wrap_from_base(int x, int N)
+{
+    if (x >= N) x -= N;
+    return x < N ? x : wrap_cell(x, N);
+}
+
 // ---- FP32 weights (mixed form) --------------------------------------------
 // sqrt(a) for a > 0 through the hardware reciprocal square root (a few ulp;
 // the mixed form's weights are FP32 values anyway), 0 for a <= 0.

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                     for (int d = 0; d < DIM; ++d)
                     {
                         const int st = (P.side && d == c) ? R0.stagger(d) : 0; // 0 or 1
-                        s0[d] = wrap_cell(R0.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + st;
+                        s0[d] = wrap_from_base(R0.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + st;
                     }
                 }
                 // Markers of the unit, software-pipelined: the next marker's
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
                     for (int d = 0; d < DIM; ++d)
                     {
                         const bool st = P.side && d == c;
-                        s0[d] = wrap_cell(R.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + (st ? R.stagger(d) : 0);
+                        s0[d] = wrap_from_base(R.bc(d) + (W - 1) / 2, P.N[d]) - org[d] + (st ? R.stagger(d) : 0);
                         weights_f32<K>(st ? R.rs[d] : R.rc[d], w[d]);
                     }
                     const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(32 * SPARSE_WARPS, 3) spread_visits_mixed(cons
 #pragma unroll
                         for (int i = 0; i < W; ++i)
                         {
-                            const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                            const int l = wrap_from_base(b + i, P.N[d]) - org[d];
                             const bool in = l >= 0 && l < T::edge(d);
                             inmask[d] |= in ? (1u << i) : 0u;
                             n += in ? 1 : 0;
@@ -675,7 +675,7 @@ __global__ void __launch_bounds__(32 * LANE_WARPS, 4) spread_visits_lanes(const 
 #pragma unroll
                 for (int i = 0; i < W; ++i)
                 {
-                    const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                    const int l = wrap_from_base(b + i, P.N[d]) - org[d];
                     off[d][i] = (l >= 0 && l < T::edge(d)) ? l * stride : -(1 << 20);
                 }
             }
@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
 #pragma unroll
                         for (int i = 0; i < W; ++i)
                         {
-                            const int l = wrap_cell(b + i, P.N[d]) - org[d];
+                            const int l = wrap_from_base(b + i, P.N[d]) - org[d];
                             // Q/vol rides on the last dimension's weights
                             if (l >= 0 && l < T::edge(d)) mine[off + l] += d == DIM - 1 ? w[i] * V : w[i];
                         }
