@@ -244,7 +244,11 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
                 base_r_fp64<K>(X, P.xlo_s[d], P.dx[d], P.inv_dx[d], P.dx_pow2[d], bs, rs);
             // Periodic domain: move both bases by the multiple of N that puts bc in [0, N).
             const int N = P.N[d];
-            const int shift = (bc >= 0 ? bc / N : -((-bc + N - 1) / N)) * N;
+            // (no division for markers within one period of the box)
+            const int shift = (bc >= 0 && bc < N)   ? 0
+                              : (bc >= N && bc < 2 * N) ? N
+                              : (bc < 0 && bc >= -N)    ? -N
+                              : (bc >= 0 ? bc / N : -((-bc + N - 1) / N)) * N;
             bc -= shift;
             bs -= shift;
             rkey |= (unsigned long long)(unsigned short)bc << (16 * d);
