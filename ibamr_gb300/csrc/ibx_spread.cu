@@ -735,12 +735,13 @@ struct GatherLayout
 
 constexpr int GATHER_WARPS = 8; // tiles (warps) per CTA of the gather form
 
-// CTAs per SM the register budget is cut for: 3 x (256 threads) with 16
-// values per lane, 1 with 32 (3D tiles of 16 x 8 x 8).
+// CTAs per SM the register budget is cut for: 4 x (256 threads) with 16
+// values per lane (64 registers: more warps to hide the record loads beat
+// the few spilled values), 1 with 32 (3D tiles of 16 x 8 x 8).
 template <int DIM, int SH>
 struct GatherOccupancy
 {
-    static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 3;
+    static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 4;
 };
 
 template <int DIM, int K, int SH>
@@ -774,16 +775,6 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
         int org[3];
         tile_origin<DIM, SH>(P, t - P.tile0, org);
         const float* Qf = static_cast<const float*>(P.Q);
-        // A tile with at most 32 visits keeps each lane's visit in registers
-        // for every component.
-        const bool one = vend - vbeg <= 32;
-        int gk = 0;
-        Rec Rk;
-        if (one && lane < vend - vbeg)
-        {
-            gk = D.visit_list[vbeg + lane];
-            Rk = D.rec[gk];
-        }
         for (int c = 0; c < P.ncomp; ++c)
         {
             float hi[CPL], lo[CPL];
@@ -797,8 +788,8 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
                 for (int i = 0; i < SS / 4; ++i) reinterpret_cast<float4*>(mine)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (lane < nb)
                 {
-                    const int g = one ? gk : D.visit_list[b0 + lane];
-                    const Rec R = one ? Rk : D.rec[g];
+                    const int g = D.visit_list[b0 + lane];
+                    const Rec R = D.rec[g];
                     const float V = Qf[(long long)P.Q_depth * (g - P.marker0) + c] * P.inv_vol;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d)
