@@ -28,7 +28,7 @@ namespace ibx
 namespace
 {
 constexpr int INTERP_THREADS = 256;
-constexpr int CHUNK = 8;      // markers per thread of interp_chunks
+constexpr int CHUNK = 4;      // markers per thread of interp_chunks
 
 // Which markers a kernel takes.
 enum Select
