@@ -2,21 +2,23 @@
 //
 // Two kernels, run in this order:
 //  - dense home tiles (more than dense_min markers): one CTA per work item
-//    (item_units home units of one tile, one thread per unit and component;
-//    a unit is a run of markers sharing every stencil base, typically
-//    consecutive markers of a fibre).  A unit's contributions are summed in FP32
-//    registers over its whole W^d footprint and merged once, with
-//    compensated shared atomics (Knuth TwoSum on the returned old value),
-//    into a double-FP32 region covering the tile and its stencil halo; the
-//    region is then added to the grid with FP32 global atomics (each grid
-//    value receives at most 2^d region sums).  Every dense-homed marker is
-//    processed exactly once.
-//  - every tile visited by sparse-homed markers: one warp per tile; lanes
-//    take visits and merge each in-tile contribution with compensated shared
-//    atomics, then the warp adds the tile's double-FP32 sums to the grid with
-//    one coalesced read-modify-write per value (compensated FP32 merge,
-//    within one FP32 ulp of the exact sum).  The warp owns its tile's values;
-//    the dense kernel's atomics have completed before it starts.
+//    (item_units home units of one tile, sorted by length; one thread per
+//    unit, component and z-slice of the footprint; a unit is a run of
+//    markers sharing every stencil base, typically consecutive markers of a
+//    fibre).  A unit's contributions are summed in FP32 registers over its
+//    footprint and merged once, with compensated shared atomics (Knuth
+//    TwoSum on the returned old value), into a double-FP32 region covering
+//    the tile and its stencil halo; the region is then added to the grid
+//    with FP32 global atomics (each grid value receives at most 2^d region
+//    sums).  Every dense-homed marker is processed exactly once.
+//  - every tile visited by sparse-homed markers: one warp per tile, in one
+//    of three forms (ibx_plan_set_visit_kernel): the tile gathered in
+//    registers from the visits' separable weights (form 2), or the visits'
+//    in-tile points merged with compensated shared atomics (forms 0 and 1).
+//    The warp then adds the tile's double-FP32 sums to the grid with one
+//    coalesced read-modify-write per value (compensated FP32 merge, within
+//    one FP32 ulp of the exact sum).  The warp owns its tile's values; the
+//    dense kernel's atomics have completed before it starts.
 //
 // Product order per contribution: w0 * (w1 * (w2 * (Q/vol))), the
 // association of the reference's tensor-product kernels (F3D:1436-1468).
