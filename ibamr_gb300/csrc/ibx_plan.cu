@@ -6,13 +6,14 @@
 //      bases and kernel arguments (cell-centred and staggered position) and
 //      counts the marker into its home tile (warp-aggregated atomics).
 //   2. exclusive scans (exact integer).
-//   3. counting sort by home tile; markers of sparse home tiles count the
+//   3. counting sort by home tile, which also cuts dense home tiles into
+//      work items of home units; markers of sparse home tiles count the
 //      tiles their footprints touch; scans; counting sort of those visits.
-//   4. work items: dense home tiles are split into items of home units.
-//   5. spread (ibx_spread.cu): dense tiles spread their home markers into a
+//   4. spread (ibx_spread.cu): dense tiles spread their home markers into a
 //      tile+halo region, sparse-homed markers are spread by the owner of
 //      every tile they visit.
-//   6. interpolate (ibx_interp.cu): markers in home-tile order.
+//   5. interpolate (ibx_interp.cu): markers in home-tile (or marker) order,
+//      concurrently with the spread in ibx_plan_step.
 // Geometry: IBX_MODE_PERIODIC problems (compact periodic arrays).
 
 #include "ibx_plan.cuh"
