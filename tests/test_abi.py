@@ -51,6 +51,25 @@ def test_every_declared_symbol_is_exported(libibx):
         getattr(L, n)
 
 
+def test_plan_knobs_reject_a_null_plan(libibx):
+    """The plan setters validate on the host (no device call): a null plan is
+    an argument error, the getters answer -1."""
+    L = ctypes.CDLL(libibx)
+    E_ARG = 4
+    for setter in ("ibx_plan_set_visit_kernel", "ibx_plan_set_interp_kernel", "ibx_plan_set_step_mode",
+                   "ibx_plan_set_unit_cap"):
+        fn = getattr(L, setter)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        assert fn(None, 1) == E_ARG, setter
+    for getter in ("ibx_plan_get_visit_kernel", "ibx_plan_get_interp_kernel", "ibx_plan_get_step_mode",
+                   "ibx_plan_get_unit_cap"):
+        fn = getattr(L, getter)
+        fn.argtypes = [ctypes.c_void_p]
+        assert fn(None) == -1, getter
+    L.ibx_plan_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    assert L.ibx_plan_set_tuning(None, 128, 32, 2) == E_ARG
+
+
 def test_host_queries(libibx):
     L = ctypes.CDLL(libibx)
     L.ibx_status_string.restype = ctypes.c_char_p
