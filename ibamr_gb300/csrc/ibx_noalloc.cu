@@ -1,18 +1,22 @@
 // ibx_noalloc.cu -- binned mixed-precision spreading without any device
 // allocation (ibx_spread_noalloc in include/ibx.h).
 //
-// Some callers cannot call cudaMalloc at all: code that runs while a CUDA
-// graph is being captured with a fixed memory footprint, host code inside a
-// real-time or fault-handling path, or an embedding that forbids the CUDA
-// allocator (for instance because a separate pool owns all device memory).
-// For them the scratch memory of the binned pipeline (stencil records,
-// tile counters, counting-sort lists, run units) lives in one file-scope
-// __device__ array of fixed size, which every GPU that loads this library
-// holds until the process exits.  The inputs and outputs stay the caller's.
+// Some callers cannot call cudaMalloc at all: host code inside a real-time
+// or fault-handling path, where an allocation may block on the driver or
+// fail when memory is short, and embeddings whose own pool manager owns all
+// of the device memory so that a library may not allocate beside it.  For
+// them the scratch memory of the binned pipeline (stencil records, tile
+// counters, counting-sort lists, run units, the problem descriptor) lives in
+// one file-scope __device__ array of fixed size, which every GPU that loads
+// this library holds until the process exits.  The inputs and outputs stay
+// the caller's.
 //
 // Set-up: the first call on each device, with that device current, looks up
-// the array's device address with cudaGetSymbolAddress and caches it.  Make
-// that first call before any stream capture.
+// the array's device address with cudaGetSymbolAddress and caches it.
+//
+// The problem descriptor and the offset tables reach the array through the
+// arguments of a small kernel (copied by the launch itself), so no host
+// buffer has to outlive the call.
 //
 // All calls share the one array and it keeps the contents of the last call:
 // every call re-initialises what must start at zero, and calls whose work
@@ -58,6 +62,31 @@ scratch_address(void** out)
     return IBX_OK;
 }
 
+// Descriptor of the call, written into the scratch array by one thread:
+// the problem, the marker offsets {0, n}, the tile offsets {0, n_tiles} and
+// a cleared status word.  Everything arrives as launch arguments.
+__global__ void
+noalloc_setup(ibx::PlanProb P, long long n_markers, int n_tiles, ibx::PlanProb* probs, long long* moffs, int* toffs,
+              int* status)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    *probs = P;
+    moffs[0] = 0;
+    moffs[1] = n_markers;
+    toffs[0] = 0;
+    toffs[1] = n_tiles;
+    status[0] = 0;
+}
+
+// The binning's status word as an IBX status code in the caller's int.
+__global__ void
+noalloc_report(const int* word, int* out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int w = *word;
+    *out = (w & 1) ? IBX_E_NONFINITE : (w & 2) ? IBX_E_TOO_LARGE : IBX_OK;
+}
+
 } // namespace
 
 namespace ibx
@@ -66,7 +95,7 @@ int build_prob(const ibx_problem& in, int kernel, bool spread, Prob& P);
 }
 
 extern "C" int
-ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
+ibx_spread_noalloc(const ibx_problem* problem, int kernel, int* status, void* stream)
 {
     using namespace ibx;
     if (!problem) return IBX_E_ARG;
@@ -89,7 +118,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     P.ncomp = ncomp;
     P.side = in.centering == IBX_SIDE;
     P.Q_depth = in.Q_depth;
-    long long ntiles = 1, vol = 1;
+    long long ntiles = 1, vol = 1, per = 1;
     bool fixed_ok = true;
     for (int d = 0; d < 3; ++d)
     {
@@ -111,6 +140,11 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
         P.xlo_c[d] = in.x_lower[d];
         P.xlo_s[d] = in.x_lower[d] - 0.5 * in.dx[d];
         fixed_ok = fixed_dim(in.x_lower[d], in.x_upper[d], in.dx[d], P.fx[d]) && fixed_ok;
+        // Tiles one footprint can touch along d: two, or three when the last
+        // tile is partial (a footprint at the periodic seam straddles the
+        // partial tile and both of its neighbours); never more than exist.
+        const int bound = 2 + (P.N[d] % Ed[d] != 0);
+        per *= P.ntile[d] < bound ? P.ntile[d] : bound;
     }
     if (ntiles > NOALLOC_MAX_TILES) return IBX_E_TOO_LARGE;
     P.fixed_ok = fixed_ok ? 1 : 0;
@@ -128,7 +162,8 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     P.tile0 = 0;
     P.marker0 = 0;
 
-    // Carve the scratch array (the buffers of a plan, capacities at the limits).
+    // Carve the scratch array (the buffers of a plan, with the capacities
+    // ibx_plan_create would reserve for this problem).
     const long long nm = in.n_markers;
     const int nt = (int)ntiles;
     PlanSizes z;
@@ -136,7 +171,7 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     z.n_probs = 1;
     z.n_markers = nm;
     z.n_tiles = nt;
-    z.visit_cap = nm * (dim == 3 ? 8 : 4);
+    z.visit_cap = nm * per;
     z.item_cap = nt + nm / 10 + 1;
     DevPlan D{};
     if (carve_plan(z, nullptr, D).bytes > NOALLOC_SCRATCH_BYTES) return IBX_E_TOO_LARGE;
@@ -151,17 +186,20 @@ ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream)
     if (D.item_units < 32) D.item_units = 32; // at least the units per item the capacity assumes
     D.max_ncomp = ncomp;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const long long moffs[2] = { 0, nm };
-    const int toffs[2] = { 0, nt };
-    // The pageable sources are staged by the runtime before these calls return.
-    if (cudaMemcpyAsync(b + c.o_probs, &P, sizeof(P), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b + c.o_moffs, moffs, sizeof(moffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b + c.o_toffs, toffs, sizeof(toffs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(b + c.o_status, 0, sizeof(int) * 4, s) != cudaSuccess)
-        return IBX_E_CUDA;
+    noalloc_setup<<<1, 1, 0, s>>>(P, nm, nt, reinterpret_cast<PlanProb*>(b + c.o_probs),
+                                  reinterpret_cast<long long*>(b + c.o_moffs), reinterpret_cast<int*>(b + c.o_toffs),
+                                  reinterpret_cast<int*>(b + c.o_status));
+    note_launches(1);
+    if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
 
     // Counters and cursors are zeroed by the binning sequence on every call.
     int rc = bin_sequence(dim, kernel, D, c.scan_tmp, s);
     if (!rc) rc = launch_spread(dim, kernel, D, ncomp, s);
+    if (!rc && status)
+    {
+        noalloc_report<<<1, 1, 0, s>>>(D.status, status);
+        note_launches(1);
+        if (cudaGetLastError() != cudaSuccess) rc = IBX_E_CUDA;
+    }
     return rc;
 }

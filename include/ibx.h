@@ -303,23 +303,32 @@ int ibx_plan_destroy(ibx_plan* plan);
 /* ---- allocation-free spreading ----------------------------------------- */
 /* No counterpart in the reference (IBAMR's LEInteractor runs on the CPU and
  * allocates freely); it exists for callers of this library that cannot
- * allocate device memory: code running while a CUDA graph is captured with a
- * fixed memory footprint, real-time or error-handling paths, and embeddings
- * whose memory pool owns the whole device so that cudaMalloc is not
- * available to libraries.
+ * allocate device memory: real-time or fault-handling host paths, where a
+ * cudaMalloc may block on the driver or fail when memory is short, and
+ * embeddings whose own memory pool owns the whole device, so that a library
+ * may not allocate beside it.
  *
  * ibx_spread_noalloc: the binned mixed-precision spread of ibx_plan_bin +
  * ibx_plan_spread for one IBX_MODE_PERIODIC problem (float q and Q), with
  * every scratch buffer placed in a fixed 8 MiB array inside the library
  * (held on every GPU that loads it until the process exits).  It calls no
  * allocating routine.  Limits: at most IBX_NOALLOC_MAX_MARKERS markers and
- * IBX_NOALLOC_MAX_TILES grid tiles (8^3 cells in 3D, 16^2 in 2D); larger
- * problems return IBX_E_TOO_LARGE.  The first call on a device looks up the
- * array's address (make it before any stream capture).  All calls share the
- * array: calls whose work overlaps on the GPU race and must be serialised. */
+ * IBX_NOALLOC_MAX_TILES grid tiles (8^3 cells in 3D, 16^2 in 2D), and the
+ * scratch the problem needs must fit the array (grids whose cell count is
+ * not a multiple of the tile edge need more visit slots per marker); larger
+ * problems return IBX_E_TOO_LARGE and nothing is launched.  The first call
+ * on a device, with that device current, looks up the array's address.  All
+ * calls share the array, which keeps the last call's contents: each call
+ * clears what must start at zero, and calls whose work overlaps on the GPU
+ * race and must be serialised.
+ *
+ * status: a DEVICE int, or NULL.  When given, it receives, in stream order
+ * after the spread, IBX_OK, IBX_E_NONFINITE (a marker position was NaN or
+ * infinite; that marker was skipped) or IBX_E_TOO_LARGE (a list capacity
+ * overflowed; the result is incomplete). */
 #define IBX_NOALLOC_MAX_MARKERS 32768
 #define IBX_NOALLOC_MAX_TILES 4096
-int ibx_spread_noalloc(const ibx_problem* problem, int kernel, void* stream);
+int ibx_spread_noalloc(const ibx_problem* problem, int kernel, int* status, void* stream);
 
 #ifdef __cplusplus
 }
