@@ -3,20 +3,26 @@
 
 Metric: spread + interpolate markers/s (one step = bin the markers, spread
 their forces onto the staggered grid, interpolate the staggered velocity
-back onto them).  Workload: 2,000,000 markers (64 helical fibres packed in a
-0.2^3 sub-box + 400k uniform) on a 256^3 periodic staggered grid, IB_4
-kernel, mixed precision (FP32 values, FP64 positions / indices / kernel
-arguments, double-FP32 spread accumulation).  The plain FP64 form on the same
-workload, the error against it, the CPU baseline, the end-to-end rate with
-host buffers and the roofline of the dominant kernel are reported on the
-same JSON line.
+back onto them).  Headline workload: 2,000,000 markers (64 helical fibres
+packed in a 0.2^3 sub-box + 400k uniform) on a 256^3 periodic staggered
+grid, IB_4 kernel, mixed precision (FP32 values, FP64 positions / indices /
+kernel arguments, double-FP32 spread accumulation).  The plain FP64 form on
+the same workload, the error against it, the CPU baseline, the end-to-end
+rate with host buffers and the roofline of the dominant kernel are reported
+on the same JSON line, and nested objects carry the other measured
+configurations: ``ib6`` (the same workload with IB_6), ``batched`` (512
+independent 2D problems, one CUDA graph per step, autotuned) and ``serving``
+(Poisson request stream over resident simulations, p50/p99 latency).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--workload helices|batched|serving]
+                  [--workload all|helices|batched|serving] [--kernel K]
+                  [--setting k=v,...] [--tune]
 
---workload batched: 512 independent 2D periodic problems (N uniform in
-{32..512}, 100-20,000 markers each on random closed curves) stepped as one
-CUDA graph; --workload serving: the request loop of ibamr_gb300.serving.
+The helices workload runs with the plan setting recorded in
+profiles/traffic.json (the autotuner's choice, profiled with ncu there, so
+that roofline.traffic describes the benched schedule); --tune re-runs the
+autotuner instead, --setting fixes another setting.  The batched workload is
+always autotuned (tile shape and knobs), as its configuration asks.
 
 Multi-GPU: replicas only (each rank runs the whole workload on its GPU,
 value = sum over ranks, "scaling": "weak").
@@ -28,7 +34,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -38,18 +43,18 @@ import numpy as np  # noqa: E402
 
 METRIC = "spread+interp markers/s"
 UNIT = "markers/s"
-KERNEL = "IB_4"
-KERNEL_W = 4
 KERNEL_WIDTHS = {"IB_3": 3, "IB_4": 4, "IB_6": 6, "PIECEWISE_CUBIC": 4, "BSPLINE_4": 4, "PIECEWISE_LINEAR": 2}
 N_GRID = 256
-WORKLOAD = "helices64x25k+uniform400k_256cube_IB4"
+DTYPE = "mixed: f32 values, f64 positions/indices, double-f32 accumulation"
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
 
 
-def use_kernel(name):
-    """Select the delta kernel of the helices workload (names its workload)."""
-    global KERNEL, KERNEL_W, WORKLOAD
-    KERNEL, KERNEL_W = name, KERNEL_WIDTHS[name]
-    WORKLOAD = "helices64x25k+uniform400k_256cube_" + name.replace("_", "")
+def helices_workload(kernel):
+    return "helices64x25k+uniform400k_256cube_" + kernel.replace("_", "")
+
+
+BATCH_WORKLOAD = "batched512_2d_N32-512_markers100-20000_fourier_IB4"
+SERVE_WORKLOAD = "serving_poisson2000_32sims_2d64-512_3d32-192_markers1e3-5e5_IB4_budget150GB"
 
 
 def parse_args():
@@ -58,16 +63,16 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample", type=float, default=0.1, help="fraction of markers for the CPU baseline")
-    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
+    ap.add_argument("--tune", action="store_true", help="run the autotuner on the helices workload")
+    ap.add_argument("--no-tune", action="store_true", help="library defaults on the helices workload")
     ap.add_argument("--setting", default=None,
-                    help="fixed plan setting k=v,... as printed under tuning.setting (skips the autotuner)")
+                    help="fixed plan setting k=v,... as printed under tuning.setting (helices workload)")
     ap.add_argument("--kernel", default="IB_4", choices=sorted(KERNEL_WIDTHS),
-                    help="delta kernel of the helices workload (the metric is quoted on IB_4; the same "
-                         "configuration also runs IB_6)")
-    ap.add_argument("--workload", default="helices", choices=["helices", "batched", "serving"],
-                    help="helices: 2M markers on 256^3 (default); batched: 512 independent 2D problems in one "
-                         "CUDA graph; serving: Poisson request stream over resident simulations")
+                    help="delta kernel of the helices workload (the metric is quoted on IB_4)")
+    ap.add_argument("--workload", default="all", choices=["all", "helices", "batched", "serving"],
+                    help="all: the helices line (IB_4) with nested ib6, batched and serving results; "
+                         "helices / batched / serving: that workload's line alone")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines (profiling runs)")
     return ap.parse_args()
 
 
@@ -94,6 +99,15 @@ def measured_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def recorded_traffic():
+    """profiles/traffic.json: {workload: {"setting": ..., "spread": bytes, ...}}."""
+    try:
+        with open(TRAFFIC) as f:
+            return json.load(f)
+    except Exception:
+        return {}
 
 
 class ClockSampler:
@@ -144,6 +158,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def cuda_timer(stream):
+    import torch
+
+    def timed(fn, reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    return timed
+
+
+# ---------------------------------------------------------------------------
+# CPU baselines (the reference's per-patch CPU path, oracle port)
+# ---------------------------------------------------------------------------
 def make_markers():
     from ibamr_gb300 import workloads
 
@@ -153,116 +187,158 @@ def make_markers():
     return X, F
 
 
-def cpu_baseline(X, F, u_np, fraction, steps=2):
-    """The reference's per-patch CPU path (oracle port, one thread per slab
-    patch) on a bounded sample of the markers; markers/s."""
+def helices_cpu(X, F, u_np, kernel, steps, warmup):
+    """The reference's per-patch CPU flow on the whole helices workload: box
+    patches cut by marker workload, four per host thread, worked through by
+    every host thread; markers/s."""
     from oracle import ibx_oracle as oracle
 
     n = X.size // 3
-    m = max(1000, int(n * fraction))
-    rng = np.random.default_rng(7)
-    sel = np.sort(rng.choice(n, size=m, replace=False))
-    Xs = np.ascontiguousarray(X.reshape(n, 3)[sel].reshape(-1))
-    Fs = np.ascontiguousarray(F.reshape(n, 3)[sel].reshape(-1))
     cores = os.cpu_count() or 1
-    plan = oracle.CpuPlan(3, [N_GRID] * 3, KERNEL, Xs, cores)
+    plan = oracle.CpuPlan(3, [N_GRID] * 3, kernel, X, threads=cores, boxes=4 * cores)
     f = np.zeros(3 * N_GRID ** 3)
-    U = np.zeros(Xs.size)
-    plan.step(Fs, f, u_np, U)  # warm-up
+    U = np.zeros(X.size)
+    for _ in range(warmup):
+        plan.step(F, f, u_np, U)
     t0 = time.perf_counter()
     for _ in range(steps):
-        plan.step(Fs, f, u_np, U)
+        plan.step(F, f, u_np, U)
     dt = (time.perf_counter() - t0) / steps
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "whole workload (%d markers, %d^3 grid) per step, %d box patches on %d threads, %d timed "
+                      "steps" % (n, N_GRID, plan.patches, cores, steps), "ms_per_step": dt * 1e3}
+
+
+def batched_problems():
+    from ibamr_gb300 import workloads
+
+    return [([N, N], X) for N, X in workloads.batched_2d(512)]
+
+
+def batched_cpu(problems, F, steps=1, warmup=1):
+    """The per-patch CPU path on every problem of the batch, one problem per
+    task on a pool of host threads; markers/s."""
+    import concurrent.futures
+
+    from oracle import ibx_oracle as oracle
+
+    moff = np.concatenate([[0], np.cumsum([X.size // 2 for _, X in problems])])
+    cores = os.cpu_count() or 1
+    work = []
+    for k, (N, X) in enumerate(problems):
+        vol = N[0] * N[1]
+        Fk = np.ascontiguousarray(F[2 * moff[k]: 2 * moff[k + 1]])
+        u = np.random.default_rng(100 + k).standard_normal(2 * vol)
+        work.append((oracle.CpuPlan(2, N, "IB_4", X), Fk, np.zeros(2 * vol), u, np.zeros(X.size)))
+
+    def run(w):
+        plan, Fk, f, u, U = w
+        plan.step(Fk, f, u, U)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
+        for _ in range(warmup):
+            list(ex.map(run, work))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            list(ex.map(run, work))
+        dt = (time.perf_counter() - t0) / steps
+    m = int(moff[-1])
     return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of %d markers (uniform subsample), full %d^3 grid, %d slab patches, %d timed steps"
-                      % (m, n, N_GRID, cores, steps), "ms_per_step": dt * 1e3}
+            "sample": "all %d problems (%d markers) per step, one problem per task on %d threads, %d timed steps"
+                      % (len(problems), m, cores, steps), "ms_per_step": dt * 1e3}
 
 
-def run_reference_other(args, world):
-    """Reference arm of the batched and serving workloads: the oracle port of
-    the per-patch CPU path over a sample of the same problems."""
+def serving_specs(n_sims=32):
+    from ibamr_gb300 import serving, workloads
+
+    return [serving.SimSpec(sid, dim, N, X, F=F, u=u) for sid, dim, N, X, F, u in workloads.serving_mix(n_sims)]
+
+
+def serving_cpu(specs):
+    """The per-patch CPU path for one request of every simulation, one
+    simulation per task on a pool of host threads; markers/s."""
+    import concurrent.futures
+
+    from oracle import ibx_oracle as oracle
+
+    cores = os.cpu_count() or 1
+    work = []
+    for s in specs:
+        vol = int(np.prod(s.N))
+        work.append((oracle.CpuPlan(s.dim, s.N, "IB_4", s.X), np.ascontiguousarray(s.F, dtype=np.float64),
+                     np.zeros(s.dim * vol), np.ascontiguousarray(s.u, dtype=np.float64).reshape(-1),
+                     np.zeros(s.X.size)))
+
+    def run(w):
+        plan, F, f, u, U = w
+        plan.step(F, f, u, U)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(run, work))
+        t0 = time.perf_counter()
+        list(ex.map(run, work))
+        dt = time.perf_counter() - t0
+    m = int(sum(s.n_markers for s in specs))
+    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "one request of each of the %d simulations (%d markers), one simulation per task on %d "
+                      "threads" % (len(specs), m, cores), "ms_per_step": dt * 1e3}
+
+
+# ---------------------------------------------------------------------------
+# Reference arm: the CPU port of the reference's per-patch flow
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
     from ibamr_gb300 import workloads
 
     if args.workload == "batched":
         problems = batched_problems()
         nm = sum(X.size // 2 for _, X in problems)
         F = np.random.default_rng(workloads.SEED + 40).standard_normal(nm * 2)
-        cpu = batched_cpu_baseline(problems, F, 64, steps=max(1, args.steps // 10), warmup=1)
-        workload = BATCH_WORKLOAD
+        cpu = batched_cpu(problems, F, steps=args.steps, warmup=args.warmup)
+        config = {"workload": BATCH_WORKLOAD, "kernel": "IB_4"}
+    elif args.workload == "serving":
+        cpu = serving_cpu(serving_specs())
+        config = {"workload": SERVE_WORKLOAD, "kernel": "IB_4"}
     else:
-        cpu = serving_cpu_baseline(serving_specs())
-        workload = SERVE_WORKLOAD
+        X, F = make_markers()
+        u_np = np.random.default_rng(11).standard_normal(3 * N_GRID ** 3)
+        cpu = helices_cpu(X, F, u_np, args.kernel, steps=args.steps, warmup=args.warmup)
+        config = {"workload": helices_workload(args.kernel), "markers": X.size // 3, "grid": [N_GRID] * 3,
+                  "kernel": args.kernel}
     line = {
         "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": cpu["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload, "kernel": KERNEL},
-        "cpu_baseline": cpu,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config,
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_reference(args):
-    rank, _, world = dist_env()
-    if rank != 0:
-        return
-    if args.workload != "helices":
-        return run_reference_other(args, world)
-    X, F = make_markers()
-    rng = np.random.default_rng(11)
-    u_np = rng.standard_normal(3 * N_GRID ** 3)
-    from oracle import ibx_oracle as oracle
-
-    n = X.size // 3
-    frac = args.cpu_sample
-    m = max(1000, int(n * frac))
-    sel = np.sort(np.random.default_rng(7).choice(n, size=m, replace=False))
-    Xs = np.ascontiguousarray(X.reshape(n, 3)[sel].reshape(-1))
-    Fs = np.ascontiguousarray(F.reshape(n, 3)[sel].reshape(-1))
-    cores = os.cpu_count() or 1
-    plan = oracle.CpuPlan(3, [N_GRID] * 3, KERNEL, Xs, cores)
-    f = np.zeros(3 * N_GRID ** 3)
-    U = np.zeros(Xs.size)
-    for _ in range(args.warmup):
-        plan.step(Fs, f, u_np, U)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        plan.step(Fs, f, u_np, U)
-    dt = (time.perf_counter() - t0) / args.steps
-    value = m / dt
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "markers": n, "grid": [N_GRID] * 3, "kernel": KERNEL},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d of %d markers per step (uniform subsample), %d slab patches" % (m, n, cores)},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-
-
-def run_ours(args):
+# ---------------------------------------------------------------------------
+# Helices workload (the headline configuration, and IB_6)
+# ---------------------------------------------------------------------------
+def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup):
+    """One kernel on the 2M-marker workload: tuned or pinned plan, timed
+    steps, phases, roofline, accuracy against the plain FP64 form, plain FP64
+    rate, end to end with host buffers, CPU baseline."""
     import torch
 
-    from ibamr_gb300 import ibx, workloads
+    from ibamr_gb300 import ibx, tuning, workloads
 
-    rank, local_rank, world = dist_env()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
-    ibx.lib()
+    rank = dist_env()[0]
+    W = KERNEL_WIDTHS[kernel]
+    workload = helices_workload(kernel)
     X, F = make_markers()
     n = X.size // 3
     N = [N_GRID] * 3
     dx = [1.0 / N_GRID] * 3
-    rng = np.random.default_rng(11)
-    u_np = rng.standard_normal(3 * N_GRID ** 3)
+    u_np = np.random.default_rng(11).standard_normal(3 * N_GRID ** 3)
     stream = torch.cuda.current_stream()
+    timed = cuda_timer(stream)
 
     X_t = torch.tensor(X, device=dev)
     F_t = torch.tensor(F, dtype=torch.float32, device=dev)
@@ -275,33 +351,39 @@ def run_ours(args):
                                 q, Xq, Q)
 
     def make_plan(shape):
-        return ibx.Plan(prob(f_t, X_t, F_t), KERNEL, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)],
+        return ibx.Plan(prob(f_t, X_t, F_t), kernel, ibx.MIXED, interp_problems=[prob(u_t, X_t, U_t)],
                         tile_shape=shape)
 
-    from ibamr_gb300 import tuning
-
-    tuned = None
-    if args.setting:
-        fixed = tuning.parse_setting(args.setting)
+    recorded = recorded_traffic().get(workload)
+    tuned, source = None, "library defaults"
+    if setting_mode == "tune":
+        plan, tuned = tuning.autotune_shape(make_plan, reps=8)
+        source = "autotuner"
+    elif isinstance(setting_mode, str) and setting_mode not in ("defaults", "pinned"):
+        fixed = tuning.parse_setting(setting_mode)
         plan = make_plan(fixed.get("tile_shape", 0))
         tuning.apply_setting(plan, fixed)
-    elif args.no_tune:
-        plan = make_plan(0)
-    else:
+        source = "fixed"
+    elif setting_mode == "pinned" and recorded and recorded.get("setting"):
+        fixed = tuning.parse_setting(recorded["setting"])
+        plan = make_plan(fixed.get("tile_shape", 0))
+        tuning.apply_setting(plan, fixed)
+        source = "autotuner's choice recorded with the ncu profile (profiles/traffic.json)"
+    elif setting_mode == "pinned":
         plan, tuned = tuning.autotune_shape(make_plan, reps=8)
+        source = "autotuner"
+    else:
+        plan = make_plan(0)
     setting = tuning.setting_string(tuning.setting_of(plan))
-
-    def step():
-        plan.step()  # bin, then spread and interpolate concurrently
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(args.warmup):
-        step()
+    for _ in range(warmup):
+        plan.step()
     torch.cuda.synchronize()
-    sampler = ClockSampler(local_rank)
+    sampler = ClockSampler(dev.index or 0)
     sampler.start()
     barrier()
     torch.cuda.synchronize()
@@ -310,70 +392,57 @@ def run_ours(args):
     launches0 = ibx.kernel_launches()
     torch.cuda.nvtx.range_push("timed_steps")  # profilers can select the timed launches by this range
     e0.record(stream)
-    for _ in range(args.steps):
-        step()
+    for _ in range(steps):
+        plan.step()  # bin, then spread and interpolate concurrently
     e1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     launches = ibx.kernel_launches() - launches0
     barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = max_over_ranks(ms, world, dev)
+    ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, dev)
     value = world * n / (ms * 1e-3)
 
-    # ---- per-phase timing (same stream) for the roofline --------------------
-    def timed(fn, reps):
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(stream)
-        for _ in range(reps):
-            fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / reps
-
-    reps = max(3, args.steps // 2)
+    # per-phase timing (same stream) for the roofline
+    reps = max(3, steps // 2)
     t_bin = timed(plan.bin, reps)
     t_spread = timed(plan.spread, reps)
     t_interp = timed(plan.interpolate, reps)
-    T = workloads.touched_faces(X, 3, N, KERNEL_W)
+    T = workloads.touched_faces(X, 3, N, W)
     s_v = s_g = 4
     b_spread = n * 3 * (8 + s_v) + T * 2 * s_g
     b_interp = n * 3 * (8 + s_v) + T * s_g
     b_step = n * 3 * (8 + 2 * s_v) + T * 3 * s_g
-    peak, peak_kind = measured_peak()
     b_bin = n * 3 * 8  # binning reads the positions once
+    peak, peak_kind = measured_peak()
     dom = max([("spread", t_spread, b_spread), ("interpolate", t_interp, b_interp), ("bin", t_bin, b_bin)],
               key=lambda z: z[1])
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get(dom[0])
-        except Exception:
-            traffic = None
-    achieved = (dom[2] / (dom[1] * 1e-3)) / 1e9 if dom[2] else 0.0
+    traffic, traffic_note = None, "no ncu record for this setting"
+    if recorded and recorded.get("setting") == setting:
+        traffic = recorded.get(dom[0])
+        traffic_note = "ncu DRAM bytes of the %s phase with this setting (profiles/traffic.json)" % dom[0]
+    achieved = (dom[2] / (dom[1] * 1e-3)) / 1e9
     roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note,
+                "peak_source": peak_kind,
                 "step_achieved": (b_step / (ms * 1e-3)) / 1e9, "step_frac": (b_step / (ms * 1e-3)) / 1e9 / peak,
                 "algorithmic_bytes": {"spread": b_spread, "interpolate": b_interp, "bin": b_bin, "step": b_step,
                                       "touched_faces": T}}
 
-    # ---- accuracy of the mixed form against the plain FP64 form -------------
+    # accuracy of the mixed form against the plain FP64 form
     f_t2 = [torch.zeros(N, dtype=torch.float32, device=dev) for _ in range(3)]
-    plan_e = ibx.Plan(prob(f_t2, X_t, F_t), KERNEL, ibx.MIXED, tile_shape=plan.tile_shape[0])
+    plan_e = ibx.Plan(prob(f_t2, X_t, F_t), kernel, ibx.MIXED, tile_shape=plan.tile_shape[0])
     plan_e.set_tuning(*plan.tuning())
     plan_e.visit_kernel = plan.visit_kernel
+    plan_e.unit_cap = plan.unit_cap
     plan_e.bin()
     plan_e.spread()
     fd = [torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3)]
     ud = [t.double() for t in u_t]
     Fd = torch.tensor(F, device=dev)
     Ud = torch.zeros(3 * n, dtype=torch.float64, device=dev)
-    ibx.spread(prob(fd, X_t, Fd), KERNEL, ibx.FP64)
-    ibx.interpolate(prob(ud, X_t, Ud), KERNEL, ibx.FP64)
+    ibx.spread(prob(fd, X_t, Fd), kernel, ibx.FP64)
+    ibx.interpolate(prob(ud, X_t, Ud), kernel, ibx.FP64)
     torch.cuda.synchronize()
     err_f = max(float((f_t2[a].double() - fd[a]).abs().max()) for a in range(3)) / max(
         float(fd[a].abs().max()) for a in range(3))
@@ -381,26 +450,24 @@ def run_ours(args):
     torch.cuda.synchronize()
     err_U = float((U_t.double() - Ud).abs().max() / Ud.abs().max())
     plan_e.close()
+    del f_t2
 
-    # ---- plain FP64 form (marker-parallel, FP64 atomics) on the same workload --
+    # plain FP64 form (marker-parallel, FP64 atomics) on the same workload
     def step_plain():
-        ibx.spread(prob(fd, X_t, Fd), KERNEL, ibx.FP64)
-        ibx.interpolate(prob(ud, X_t, Ud), KERNEL, ibx.FP64)
+        ibx.spread(prob(fd, X_t, Fd), kernel, ibx.FP64)
+        ibx.interpolate(prob(ud, X_t, Ud), kernel, ibx.FP64)
 
     step_plain()
-    k_plain = max(2, args.steps // 5)
-    ms_plain = timed(step_plain, k_plain)
+    ms_plain = timed(step_plain, max(2, steps // 5))
     del fd, ud, Fd, Ud
 
-    # ---- end to end through the public API with host buffers ----------------
+    # end to end through the public API with host buffers: the forces go up
+    # beside the binning (which needs only the positions), spread and
+    # interpolation run on two streams, the velocities come down as soon as
+    # the interpolation ends
     Xh = torch.tensor(X).pin_memory()
     Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
     Uh = torch.empty(3 * n, dtype=torch.float32).pin_memory()
-
-    # The step's copies overlap its work through the public API's stream
-    # arguments: the forces go up beside the binning (which needs only the
-    # positions), the spread and the interpolation run on two streams, and
-    # the velocities come down as soon as the interpolation ends.
     side = torch.cuda.Stream(device=dev)
     ev_F = torch.cuda.Event()
 
@@ -423,165 +490,91 @@ def run_ours(args):
     for _ in range(2):
         step_e2e()
     barrier()
-    ms_e2e = timed(step_e2e, args.steps)
-    ms_e2e = max_over_ranks(ms_e2e, world, dev)
+    ms_e2e = max_over_ranks(timed(step_e2e, steps), world, dev)
     e2e = {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": X.size * 8 + F.size * 4,
            "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e}
-
-    cpu = cpu_baseline(X, F, u_np, args.cpu_sample) if rank == 0 else None
-    plan_tile_edges = plan.tile_shape[1]
+    status = plan.status()
+    tile_edges = list(plan.tile_shape[1])
     plan.close()
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
-            "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "markers": n, "grid": N, "kernel": KERNEL, "centering": "side",
-                       "precision": "mixed", "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
-                       "parallelism": "replicas" if world > 1 else "single"},
-            "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
-            "plain_fp64": {"value": n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
-            "mixed_vs_plain": ms_plain / ms,
-            "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
-            "tuning": {
-                "setting": setting, "tile_edges": list(plan_tile_edges),
-                "source": "autotuner" if tuned is not None else "fixed" if args.setting else "library defaults",
-                "tuned_step_ms": None if tuned is None else tuned["ms"],
-                "per_shape": None if tuned is None else {
-                    str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks,
-        }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    del f_t, u_t, X_t, F_t, U_t
+    torch.cuda.empty_cache()
+    cpu = None
+    if with_cpu and rank == 0:
+        cpu = helices_cpu(X, F, u_np, kernel, steps=2 if kernel == "IB_4" else 1, warmup=1)
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded)",
+        "config": {"workload": workload, "markers": n, "grid": N, "kernel": kernel, "centering": "side",
+                   "precision": "mixed", "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
+        "plain_fp64": {"value": world * n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+        "mixed_vs_plain": ms_plain / ms,
+        "error_vs_fp64": {"spread": err_f, "interpolate": err_U, "tolerance": 1e-5},
+        "status": ibx.status_string(status),
+        "tuning": {
+            "setting": setting, "tile_edges": tile_edges, "source": source,
+            "tuned_step_ms": None if tuned is None else tuned["ms"],
+            "per_shape": None if tuned is None else {
+                str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clocks,
+    }
 
 
 # ---------------------------------------------------------------------------
-# Batched workload: 512 independent 2D periodic problems, one CUDA graph.
+# Batched workload: 512 independent 2D periodic problems, one CUDA graph
 # ---------------------------------------------------------------------------
-BATCH_WORKLOAD = "batched512_2d_N32-512_markers100-20000_fourier_IB4"
-
-
-def batched_problems():
-    from ibamr_gb300 import workloads
-
-    return [([N, N], X) for N, X in workloads.batched_2d(512)]
-
-
-def batched_cpu_baseline(problems, F, n_sample, steps=1, warmup=1):
-    """The per-patch CPU path (oracle port) on a bounded sample of the
-    problems, one problem per host thread; markers/s."""
-    import concurrent.futures
-
-    from oracle import ibx_oracle as oracle
-
-    rng = np.random.default_rng(17)
-    moff = np.concatenate([[0], np.cumsum([X.size // 2 for _, X in problems])])
-    sel = sorted(rng.choice(len(problems), size=min(n_sample, len(problems)), replace=False).tolist())
-    cores = os.cpu_count() or 1
-    work = []
-    for k in sel:
-        N, X = problems[k]
-        vol = N[0] * N[1]
-        Fk = np.ascontiguousarray(F[2 * moff[k]: 2 * moff[k + 1]])
-        u = np.random.default_rng(100 + k).standard_normal(2 * vol)
-        work.append((oracle.CpuPlan(2, N, KERNEL, X, 1), Fk, np.zeros(2 * vol), u, np.zeros(X.size)))
-
-    def run(w):
-        plan, Fk, f, u, U = w
-        plan.step(Fk, f, u, U)
-
-    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
-        for _ in range(warmup):
-            list(ex.map(run, work))
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            list(ex.map(run, work))
-        dt = (time.perf_counter() - t0) / steps
-    m = int(sum(problems[k][1].size // 2 for k in sel))
-    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of %d problems (%d markers), one problem per thread, %d timed steps"
-                      % (len(sel), len(problems), m, steps), "ms_per_step": dt * 1e3}
-
-
-
-def run_batched(args):
+def batched_case(args, dev, world, with_cpu, steps, warmup, setting=None):
     import torch
 
-    from ibamr_gb300 import batch, ibx, workloads
+    from ibamr_gb300 import batch, ibx, tuning, workloads
 
-    rank, local_rank, world = dist_env()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
-    ibx.lib()
+    rank = dist_env()[0]
     problems = batched_problems()
-    B = batch.BatchedProblems(problems, dim=2, kernel=KERNEL, device=dev, tune=False)
+    B = batch.BatchedProblems(problems, dim=2, kernel="IB_4", device=dev, tune=False)
     nm = int(B.marker_offsets[-1])
-    rng = np.random.default_rng(workloads.SEED + 40)
-    F = rng.standard_normal(nm * 2)
+    F = np.random.default_rng(workloads.SEED + 40).standard_normal(nm * 2)
     B.F.copy_(torch.tensor(F, dtype=torch.float32))
     gen = torch.Generator(device=dev)
     gen.manual_seed(workloads.SEED + 41)
     B.u.copy_(torch.randn(B.u.numel(), generator=gen, device=dev))
-    from ibamr_gb300 import tuning
-
-    if args.setting:
-        B.configure(tuning.parse_setting(args.setting))
-    elif not args.no_tune:
-        B.autotune(reps=8)  # on the benchmark's own forces and velocities
+    if setting:
+        B.configure(tuning.parse_setting(setting))
+    else:
+        B.autotune(reps=8)  # on the batch's own forces and velocities
     setting = tuning.setting_string(tuning.setting_of(B.plan))
     stream = torch.cuda.current_stream()
+    timed = cuda_timer(stream)
 
-    # kernels per step, counted on an eager step
     l0 = ibx.kernel_launches()
     B.step()
     per_step = ibx.kernel_launches() - l0
     B.capture()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         B.replay()
     torch.cuda.synchronize()
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    def timed(fn, reps):
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(stream)
-        for _ in range(reps):
-            fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / reps
-
-    sampler = ClockSampler(local_rank)
+    sampler = ClockSampler(dev.index or 0)
     sampler.start()
-    barrier()
+    if world > 1:
+        torch.distributed.barrier()
     torch.cuda.nvtx.range_push("timed_steps")
-    ms = timed(B.replay, args.steps)
+    ms = timed(B.replay, steps)
     torch.cuda.nvtx.range_pop()
-    barrier()
     clocks = sampler.stop()
     ms = max_over_ranks(ms, world, dev)
     value = world * nm / (ms * 1e-3)
 
-    reps = max(3, args.steps // 2)
+    reps = max(3, steps // 2)
     t_bin = timed(B.plan.bin, reps)
     t_spread = timed(B.plan.spread, reps)
     t_interp = timed(B.plan.interpolate, reps)
-    T = sum(workloads.touched_faces(X, 2, N, KERNEL_W) for N, X in problems)
+    T = sum(workloads.touched_faces(X, 2, N, 4) for N, X in problems)
     b_spread = nm * 2 * (8 + 4) + T * 2 * 4
     b_interp = nm * 2 * (8 + 4) + T * 4
     b_step = nm * 2 * (8 + 8) + T * 3 * 4
-    b_bin = nm * 2 * 8  # binning reads the positions once
+    b_bin = nm * 2 * 8
     peak, peak_kind = measured_peak()
     dom = max([("spread", t_spread, b_spread), ("interpolate", t_interp, b_interp), ("bin", t_bin, b_bin)],
               key=lambda z: z[1])
@@ -606,8 +599,8 @@ def run_batched(args):
         ip.append(mk(u64[k], U64))
 
     def step_plain():
-        ibx.spread(sp, KERNEL, ibx.FP64)
-        ibx.interpolate(ip, KERNEL, ibx.FP64)
+        ibx.spread(sp, "IB_4", ibx.FP64)
+        ibx.interpolate(ip, "IB_4", ibx.FP64)
 
     B.f.zero_()
     B.step()
@@ -616,8 +609,8 @@ def run_batched(args):
     err_f = max(float((B.grid("f", k)[a].double() - f64[k][a]).abs().max()) for k in range(len(problems))
                 for a in range(2)) / max(float(f64[k][a].abs().max()) for k in range(len(problems)) for a in range(2))
     err_U = float((B.U.double() - U64).abs().max() / U64.abs().max())
-    ms_plain = timed(step_plain, max(2, args.steps // 5))
-    del f64, u64
+    ms_plain = timed(step_plain, max(2, steps // 5))
+    del f64, u64, sp, ip, F64, U64
 
     # end to end: positions and forces in from pinned host memory, velocities out
     Xh = B.X.cpu().pin_memory()
@@ -631,118 +624,60 @@ def run_batched(args):
         Uh.copy_(B.U, non_blocking=True)
 
     step_e2e()
-    ms_e2e = timed(step_e2e, args.steps)
+    ms_e2e = max_over_ranks(timed(step_e2e, steps), world, dev)
     e2e = {"value": world * nm / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nm * 2 * (8 + 4),
            "d2h_bytes_per_step": nm * 2 * 4, "ms_per_step": ms_e2e}
-    cpu = batched_cpu_baseline(problems, F, 64) if rank == 0 else None
     tuned = B.tuning
+    status = B.status()
     B.close()
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
-            "data": "synthetic (seeded)",
-            "config": {"workload": BATCH_WORKLOAD, "problems": len(problems), "markers": nm,
-                       "grid_values": int(sum(2 * N[0] * N[1] for N, _ in problems)), "kernel": KERNEL,
-                       "centering": "side", "precision": "mixed", "launch": "one CUDA graph per step",
-                       "l2": "inputs larger than L2 (2 x 286 MB grids)",
-                       "parallelism": "replicas" if world > 1 else "single"},
-            "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
-            "plain_fp64": {"value": nm / (ms_plain * 1e-3), "ms_per_step": ms_plain},
-            "mixed_vs_plain": ms_plain / ms,
-            "error_vs_fp64": {"spread": err_f, "interpolate": err_U},
-            "tuning": {
-                "setting": setting,
-                "source": "autotuner" if tuned is not None else "fixed" if args.setting else "library defaults",
-                "per_shape": None if tuned is None else {
-                    str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * args.steps,
-            "clocks": clocks,
-        }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    torch.cuda.empty_cache()
+    cpu = batched_cpu(problems, F) if with_cpu and rank == 0 else None
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
+        "data": "synthetic (seeded)",
+        "config": {"workload": BATCH_WORKLOAD, "problems": len(problems), "markers": nm,
+                   "grid_values": int(sum(2 * N[0] * N[1] for N, _ in problems)), "kernel": "IB_4",
+                   "centering": "side", "precision": "mixed", "launch": "one CUDA graph per step",
+                   "l2": "inputs larger than L2 (2 x 286 MB grids)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
+        "plain_fp64": {"value": world * nm / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+        "mixed_vs_plain": ms_plain / ms,
+        "error_vs_fp64": {"spread": err_f, "interpolate": err_U, "tolerance": 1e-5},
+        "status": ibx.status_string(status),
+        "tuning": {
+            "setting": setting, "source": "autotuner" if tuned is not None else "fixed",
+            "tuned_step_ms": None if tuned is None else tuned["ms"],
+            "per_shape": None if tuned is None else {
+                str(k): [list(v[0]), round(v[1], 4)] for k, v in tuned["per_shape"].items()}},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": per_step * steps,
+        "kernels_per_step": per_step, "clocks": clocks,
+    }
 
 
 # ---------------------------------------------------------------------------
-# Serving workload: Poisson request stream over resident simulations.
+# Serving workload: Poisson request stream over resident simulations
 # ---------------------------------------------------------------------------
-SERVE_WORKLOAD = "serving_poisson2000_32sims_2d64-512_3d32-192_markers1e3-5e5_IB4_budget150GB"
-
-
-def serving_specs(n_sims=32):
-    from ibamr_gb300 import serving, workloads
-
-    rng = np.random.default_rng(workloads.SEED + 5)
-    specs = []
-    for sid in range(n_sims):
-        dim = 2 if rng.uniform() < 0.5 else 3
-        N = int(rng.integers(64, 513)) if dim == 2 else int(rng.integers(32, 193))
-        n = int(np.floor(np.exp(rng.uniform(np.log(1e3), np.log(5e5)))))
-        if dim == 2:
-            X = workloads.fourier_curve(n, 5000 + sid)
-        else:
-            X = workloads.fibonacci_shell(n, N, seed=6000 + sid)
-        F = rng.standard_normal(n * dim)
-        u = rng.standard_normal([dim] + [N] * dim).astype(np.float32)
-        specs.append(serving.SimSpec(sid, dim, [N] * dim, X, F=F, u=u))
-    return specs
-
-
-def serving_cpu_baseline(specs, n_sample=8):
-    """The per-patch CPU path (oracle port) for one request of each of a
-    sample of the simulations, one simulation per host thread; markers/s."""
-    import concurrent.futures
-
-    from oracle import ibx_oracle as oracle
-
-    sel = specs[:n_sample]
-    cores = os.cpu_count() or 1
-    work = []
-    for s in sel:
-        vol = int(np.prod(s.N))
-        work.append((oracle.CpuPlan(s.dim, s.N, KERNEL, s.X, 1), np.ascontiguousarray(s.F, dtype=np.float64),
-                     np.zeros(s.dim * vol), np.ascontiguousarray(s.u, dtype=np.float64).reshape(-1),
-                     np.zeros(s.X.size)))
-
-    def run(w):
-        plan, F, f, u, U = w
-        plan.step(F, f, u, U)
-
-    with concurrent.futures.ThreadPoolExecutor(max_workers=cores) as ex:
-        list(ex.map(run, work))
-        t0 = time.perf_counter()
-        list(ex.map(run, work))
-        dt = time.perf_counter() - t0
-    m = int(sum(s.n_markers for s in sel))
-    return {"value": m / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "one request of each of %d of %d simulations (%d markers), one simulation per thread"
-                      % (len(sel), len(specs), m), "ms_per_step": dt * 1e3}
-
-
-def run_serving(args):
+def serving_case(args, dev, world, with_cpu, steps):
     import torch
 
-    from ibamr_gb300 import ibx, serving
+    from ibamr_gb300 import serving, workloads
 
-    rank, local_rank, world = dist_env()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    ibx.lib()
+    rank = dist_env()[0]
     specs = serving_specs()
-    backend = serving.CudaBackend(KERNEL, device=dev)
+    backend = serving.CudaBackend("IB_4", device=dev)
     srv = serving.Server(backend, 150 * 10 ** 9, n_slots=8)
     for s in specs:
         srv.register(s)
-    n_req = max(2000, 200 * args.steps)
+    n_req = max(2000, 200 * steps)
     warm = serving.poisson_requests(2000.0, 2 * len(specs), [s.sid for s in specs], seed=1)
     warm = [serving.Request(i, 0.0, specs[i % len(specs)].sid) for i in range(len(specs))] + warm
     warm = [serving.Request(i, r.arrival, r.sid) for i, r in enumerate(warm)]
     srv.run(warm)  # every simulation resident, kernels loaded
     torch.cuda.synchronize()
     reqs = serving.poisson_requests(2000.0, n_req, [s.sid for s in specs], seed=2)
-    sampler = ClockSampler(local_rank)
+    sampler = ClockSampler(dev.index or 0)
     sampler.start()
     l0 = backend.kernel_launches  # graph replays count the kernels of the captured step
     out = srv.run(reqs)
@@ -754,55 +689,94 @@ def run_serving(args):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     srv.close()
+    torch.cuda.empty_cache()
     # algorithmic bytes of one request of each simulation (markers and
     # touched faces), summed over the saturated run's requests
-    from ibamr_gb300 import workloads
-
-    b_sim = {s.sid: s.n_markers * s.dim * (8 + 8) + 3 * 4 * workloads.touched_faces(s.X, s.dim, s.N, KERNEL_W)
+    b_sim = {s.sid: s.n_markers * s.dim * (8 + 8) + 3 * 4 * workloads.touched_faces(s.X, s.dim, s.N, 4)
              for s in specs}
     span = len(burst) / sat["requests_per_s"]
     achieved = sum(b_sim[r.sid] for r in burst) / span / 1e9
     peak, peak_kind = measured_peak()
-    cpu = serving_cpu_baseline(specs) if rank == 0 else None
+    cpu = serving_cpu(specs) if with_cpu and rank == 0 else None
+    value = world * out["markers_per_s"]
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_req,
+        "warmup": len(warm), "ms_per_step": out["mean_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded)",
+        "config": {"workload": SERVE_WORKLOAD, "simulations": len(specs), "requests": n_req,
+                   "arrival_rate_per_s": 2000.0, "slots": 8, "budget_bytes": 150 * 10 ** 9,
+                   "markers_per_simulation": "log-uniform in [1e3, 5e5]", "kernel": "IB_4",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "latency_ms": {"p50": out["p50_ms"], "p99": out["p99_ms"], "mean": out["mean_ms"]},
+        "requests_per_s": out["requests_per_s"], "max_queue": out["max_queue"],
+        "resident_bytes": out["used_bytes"], "evictions": out["evictions"],
+        "saturated": {"requests": len(burst), "markers_per_s": sat["markers_per_s"],
+                      "requests_per_s": sat["requests_per_s"], "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"]},
+        "roofline": {"bound": "hbm", "kernel": "whole request (saturated run)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "request loop through the public API; simulation state resident on the device"},
+        "gpu_launches": launches, "clocks": clocks,
+    }
+
+
+NESTED_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "phases_ms", "plain_fp64",
+               "mixed_vs_plain", "error_vs_fp64", "status", "tuning", "roofline", "e2e", "cpu_baseline",
+               "gpu_launches", "kernels_per_step", "latency_ms", "requests_per_s", "saturated", "clocks",
+               "max_queue", "resident_bytes", "evictions")
+
+
+def nested(line):
+    return {k: line[k] for k in NESTED_KEYS if k in line}
+
+
+def run_ours(args):
+    import torch
+
+    from ibamr_gb300 import ibx
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    ibx.lib()
+    with_cpu = not args.no_cpu
+    if args.setting:
+        mode = args.setting
+    elif args.tune:
+        mode = "tune"
+    elif args.no_tune:
+        mode = "defaults"
+    else:
+        mode = "pinned"
+    if args.workload == "batched":
+        line = batched_case(args, dev, world, with_cpu, args.steps, args.warmup)
+    elif args.workload == "serving":
+        line = serving_case(args, dev, world, with_cpu, args.steps)
+    else:
+        line = helices_case(args, args.kernel, dev, world, mode, with_cpu, args.steps, args.warmup)
+        if args.workload == "all":
+            line["ib6"] = nested(helices_case(args, "IB_6", dev, world, "tune", with_cpu, args.steps,
+                                              args.warmup))
+            line["batched"] = nested(batched_case(args, dev, world, with_cpu, args.steps, args.warmup))
+            line["serving"] = nested(serving_case(args, dev, world, with_cpu, args.steps))
     if rank == 0:
-        value = world * out["markers_per_s"]
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_req,
-            "warmup": len(warm), "ms_per_step": out["mean_ms"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "mixed: f32 values, f64 positions/indices, double-f32 accumulation",
-            "data": "synthetic (seeded)",
-            "config": {"workload": SERVE_WORKLOAD, "simulations": len(specs), "requests": n_req,
-                       "arrival_rate_per_s": 2000.0, "slots": 8, "budget_bytes": 150 * 10 ** 9,
-                       "markers_per_simulation": "log-uniform in [1e3, 5e5]", "kernel": KERNEL,
-                       "parallelism": "replicas" if world > 1 else "single"},
-            "latency_ms": {"p50": out["p50_ms"], "p99": out["p99_ms"], "mean": out["mean_ms"]},
-            "requests_per_s": out["requests_per_s"], "max_queue": out["max_queue"],
-            "resident_bytes": out["used_bytes"], "evictions": out["evictions"],
-            "saturated": {"requests": len(burst), "markers_per_s": sat["markers_per_s"],
-                          "requests_per_s": sat["requests_per_s"], "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"]},
-            "roofline": {"bound": "hbm", "kernel": "whole request (saturated run)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "peak_source": peak_kind},
-            "cpu_baseline": cpu,
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
-                    "note": "request loop through the public API; simulation state resident on the device"},
-            "gpu_launches": launches, "clocks": clocks,
-        }
         print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def main():
     args = parse_args()
-    if args.kernel != "IB_4":
-        if args.workload != "helices":
-            raise SystemExit("--kernel applies to the helices workload")
-        use_kernel(args.kernel)
+    if args.kernel != "IB_4" and args.workload not in ("helices", "all"):
+        raise SystemExit("--kernel applies to the helices workload")
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "batched":
-        run_batched(args)
-    elif args.workload == "serving":
-        run_serving(args)
     else:
         run_ours(args)
 

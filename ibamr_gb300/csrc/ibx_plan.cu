@@ -98,6 +98,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     const size_t o_home_units = take(sizeof(int2) * nm);
     c.o_status = take(sizeof(int) * 4);
     const size_t o_scan = take(sizeof(int) * SCAN_TMP_INTS);
+    c.o_tmaps = take(sizeof(CUtensorMap) * 3 * z.n_probs);
     c.bytes = off;
     c.scan_tmp = nullptr;
     if (!b) return c;
@@ -133,6 +134,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.tile_shape = z.tile_shape;
     D.dense_blocks_per_sm = 2;
     D.status = reinterpret_cast<int*>(b + c.o_status);
+    D.tmaps = reinterpret_cast<const CUtensorMap*>(b + c.o_tmaps);
     c.scan_tmp = reinterpret_cast<int*>(b + o_scan);
     return c;
 }
@@ -153,6 +155,7 @@ struct ibx_plan
     cudaStream_t side;
     cudaEvent_t ev_fork, ev_join;
     int step_mode;
+    int n_tma; // problems whose interpolation sources have tensor maps
 };
 
 extern "C" {
@@ -298,7 +301,15 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     }
     char* b = static_cast<char*>(dmem);
     const PlanCarve c = carve_plan(z, b, D);
-    if (cudaMemcpy(b + c.o_probs, hp.data(), sizeof(PlanProb) * n_problems, cudaMemcpyHostToDevice) != cudaSuccess ||
+    // Tensor maps of the interpolation sources (TMA-staged tile regions).
+    std::vector<CUtensorMap> maps(3 * (size_t)n_problems);
+    std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+    encode_interp_maps(dim, kernel, tile_shape, hp.data(), n_problems, maps.data());
+    int n_tma = 0;
+    for (int p = 0; p < n_problems; ++p) n_tma += hp[p].tma;
+    if (cudaMemcpy(b + c.o_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(b + c.o_probs, hp.data(), sizeof(PlanProb) * n_problems, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b + c.o_moffs, moffs.data(), sizeof(long long) * (n_problems + 1), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
         cudaMemcpy(b + c.o_toffs, toffs.data(), sizeof(int) * (n_problems + 1), cudaMemcpyHostToDevice) !=
@@ -325,6 +336,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     D.max_ncomp = max_ncomp;
     plan->dmem = dmem;
     plan->dbytes = c.bytes;
+    plan->n_tma = n_tma;
     *out = plan;
     return IBX_OK;
 }
@@ -420,7 +432,7 @@ ibx_plan_status(ibx_plan* plan, void* stream, int* status)
     if (cudaMemcpyAsync(&word, plan->D.status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess || cudaMemsetAsync(plan->D.status, 0, sizeof(int), s) != cudaSuccess)
         return IBX_E_CUDA;
-    *status = (word & 1) ? IBX_E_NONFINITE : (word & 2) ? IBX_E_TOO_LARGE : IBX_OK;
+    *status = (word & 1) ? IBX_E_NONFINITE : (word & 2) ? IBX_E_TOO_LARGE : (word & 4) ? IBX_E_TIMEOUT : IBX_OK;
     return IBX_OK;
 }
 
@@ -482,7 +494,7 @@ ibx_plan_get_step_mode(const ibx_plan* plan)
 int
 ibx_plan_set_interp_kernel(ibx_plan* plan, int form)
 {
-    if (!plan || form < 0 || form > 2) return IBX_E_ARG;
+    if (!plan || form < 0 || form > 4) return IBX_E_ARG;
     plan->D.interp_form = form;
     return IBX_OK;
 }
@@ -515,6 +527,12 @@ int
 ibx_plan_n_tiles(const ibx_plan* plan)
 {
     return plan ? plan->D.n_tiles : -1;
+}
+
+int
+ibx_plan_tma_problems(const ibx_plan* plan)
+{
+    return plan ? plan->n_tma : -1;
 }
 
 long long

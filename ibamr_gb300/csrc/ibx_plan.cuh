@@ -4,6 +4,8 @@
 
 #include "ibx_internal.h"
 
+#include <cuda.h> // CUtensorMap
+
 namespace ibx
 {
 // Tile shapes (cells per dimension), chosen per plan:
@@ -100,6 +102,7 @@ struct PlanProb
     FixedDim fx[3];
     float inv_vol;     // 1/(dx0*dx1[*dx2]) rounded to FP32
     int vec4;          // N[0] % 4 == 0 and every spread target 16-byte aligned
+    int tma;           // interior tile regions of the interpolation sources load by TMA
     const double* X;
     void* Q;           // spread source
     void* q[3];        // spread target, one array per component (side axis or cell depth)
@@ -147,11 +150,47 @@ struct DevPlan
     int max_ncomp;    // largest component count over the problems
     int zsplit;       // dense_zsplit(dim, kernel width)
     int visit_kernel; // 0: points of 32 visits flattened over lanes; 1: lane per (visit, component); 2: tile gathered
-    int interp_form;  // 0: chunks in home order; 1: dense-homed per home unit; 2: chunks in marker order
+    int interp_form;  // 0: chunks in home order; 1: dense-homed per home unit; 2: chunks in marker order;
+                      // 3: every marker from TMA-staged tile regions; 4: dense-homed from staged regions
     int unit_cap;     // most markers per home unit (1..32)
     int tile_shape;   // TileT shape id of every tile of the plan
-    int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow
+    int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow, bit 2 wait timeout
+    // Tensor maps of the interpolation sources, 3 per problem (one per
+    // component), valid where the problem's tma flag is set.
+    const CUtensorMap* tmaps;
 };
+
+// Region of an interpolation source staged for the markers homed in one
+// tile: every cell of their stencils, for both the cell-centred and the
+// staggered position.  The markers' cell-centred bases lie in [org - H,
+// org + E - 1 - H] (H = (W - 1) / 2 below the home cell), the staggered ones
+// one cell higher at most, so E + W cells per dimension cover them; along x
+// the region starts at org - 4, a 16-byte boundary (tile origins are
+// multiples of 8), and spans E + 8 cells.  CS: floats per component in
+// shared memory (a multiple of 32 so that every component starts on a
+// 128-byte boundary).
+template <int DIM, int W, int SH>
+struct IBox
+{
+    using T = TileT<DIM, SH>;
+    static constexpr int H = (W - 1) / 2;
+    static constexpr int X0 = 4; // region x origin = org - X0
+    static constexpr int BX = T::E0 + 8;
+    static constexpr int BY = T::E1 + W;
+    static constexpr int BZ = DIM == 3 ? T::E2 + W : 1;
+    static constexpr int PTS = BX * BY * BZ;
+    static constexpr int CS = (PTS + 31) / 32 * 32;
+    // highest x index: (E0 - 1) + 1 (stagger) + (W - 1) + (X0 - H) <= BX - 1
+    static_assert(W - H <= 4, "the x extent covers every stencil");
+    static_assert((BX * 4) % 16 == 0 && BX <= 256 && BY <= 256 && BZ <= 256, "TMA box rules");
+};
+
+// Host side: encodes the tensor maps of every problem's interpolation
+// sources (maps[3 * p + c]) and sets each problem's tma flag; problems whose
+// layout TMA cannot address (x extent not a multiple of 4 values, a grid
+// smaller than the box, a misaligned base) keep the flag clear and load
+// their regions with plain loads.
+void encode_interp_maps(int dim, int kernel, int tile_shape, PlanProb* probs, int n_probs, CUtensorMap* maps);
 
 // Block sums of the exclusive scans: up to 2 arrays of up to 2048 blocks.
 constexpr int SCAN_TMP_INTS = 2 * 2048;
@@ -180,7 +219,7 @@ struct PlanSizes
 };
 struct PlanCarve
 {
-    size_t bytes, o_probs, o_moffs, o_toffs, o_status;
+    size_t bytes, o_probs, o_moffs, o_toffs, o_status, o_tmaps;
     int* scan_tmp;
 };
 PlanCarve carve_plan(const PlanSizes& z, char* base, DevPlan& D);

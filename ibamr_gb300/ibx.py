@@ -79,6 +79,7 @@ def lib():
             L.ibx_plan_tile_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
             for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate", "ibx_plan_step"):
                 getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            L.ibx_plan_tma_problems.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.restype = ctypes.c_longlong
             L.ibx_plan_destroy.argtypes = [ctypes.c_void_p]
@@ -403,6 +404,12 @@ class Plan:
         if rc:
             raise IbxError(rc, "ibx_plan_get_bins")
         return bc, bs, ht, ts, hl
+
+    @property
+    def tma_problems(self):
+        """Problems whose interpolation sources load by tensor copies in the
+        staged interpolation forms (see ibx_plan_tma_problems)."""
+        return lib().ibx_plan_tma_problems(self.h)
 
     @property
     def scratch_bytes(self):

@@ -12,7 +12,9 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   CTA work item, CTAs per SM of the dense-tile kernel, and most markers per
   home unit (a unit is spread by one thread per component);
 * ``interp_kernel``: all markers in chunks (home order), dense-homed ones per
-  home unit, or all in chunks in marker order started beside the sort;
+  home unit, all in chunks in marker order started beside the sort, or
+  markers evaluated from their home tile's region staged in shared memory
+  (all of them, or the dense-homed ones);
 * ``step_mode``: spread and interpolation concurrent or one after the other
   in ``step``.
 
@@ -38,7 +40,7 @@ DEFAULT_CANDIDATES = {
     "item_units": (32, 64, 128, 256),
     "dense_blocks_per_sm": (1, 2, 4),
     "visit_kernel": (0, 1, 2),
-    "interp_kernel": (0, 1, 2),
+    "interp_kernel": (0, 1, 2, 3, 4),
     "step_mode": (1, 0),
     "unit_cap": (32, 16, 8),
 }

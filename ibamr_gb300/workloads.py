@@ -82,6 +82,28 @@ def batched_2d(n_problems=512, seed=SEED + 4):
     return out
 
 
+def serving_mix(n_sims=32, seed=SEED + 5):
+    """Resident simulations of the serving workload: each 2D with N uniform in
+    [64, 512] or 3D with N uniform in [32, 192] (equal odds), markers
+    log-uniform in [1e3, 5e5] on a Fourier curve (2D) or a Fibonacci sphere
+    shell (3D), forces and velocities N(0, 1).  Returns a list of (sid, dim,
+    N, X, F, u) with X and F FP64 and u FP32 of shape (dim,) + N[::-1]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for sid in range(n_sims):
+        dim = 2 if rng.uniform() < 0.5 else 3
+        N = int(rng.integers(64, 513)) if dim == 2 else int(rng.integers(32, 193))
+        n = int(np.floor(np.exp(rng.uniform(np.log(1e3), np.log(5e5)))))
+        if dim == 2:
+            X = fourier_curve(n, 5000 + sid)
+        else:
+            X = fibonacci_shell(n, N, seed=6000 + sid)
+        F = rng.standard_normal(n * dim)
+        u = rng.standard_normal([dim] + [N] * dim).astype(np.float32)
+        out.append((sid, dim, [N] * dim, X, F, u))
+    return out
+
+
 def touched_faces(X, dim, N, kernel_width, side=True):
     """|T|: distinct grid values inside the support of at least one marker
     (per component, summed), computed with torch on the markers' device."""

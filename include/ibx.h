@@ -238,7 +238,9 @@ int ibx_plan_spread(ibx_plan* plan, void* stream);
 int ibx_plan_interpolate(ibx_plan* plan, void* stream);
 /* Status of the marker data seen by the last ibx_plan_bin (synchronises
  * the stream, then clears the word): IBX_OK, IBX_E_NONFINITE (a position
- * was NaN or infinite; that marker was skipped) or IBX_E_TOO_LARGE. */
+ * was NaN or infinite; that marker was skipped), IBX_E_TOO_LARGE (a list
+ * capacity overflowed) or IBX_E_TIMEOUT (a bounded wait for a staged copy
+ * gave up; the interpolated values are incomplete). */
 int ibx_plan_status(ibx_plan* plan, void* stream, int* status);
 /* Copy the binning of the last ibx_plan_bin to host arrays (any may be
  * NULL; synchronises the device).  Markers are numbered across problems in
@@ -278,8 +280,13 @@ int ibx_plan_get_visit_kernel(const ibx_plan* plan);
  * unit's stencil values loaded once, every marker of the unit summed from
  * them), the others in chunks; 2 = every marker in chunks in the caller's
  * marker order, which needs only the stencil records, so that
- * ibx_plan_step (concurrent mode) starts it beside the counting sort.  Every
- * form sums in the same order: identical results. */
+ * ibx_plan_step (concurrent mode) starts it beside the counting sort;
+ * 3 = every marker from its home tile's region of the grid staged in shared
+ * memory (tensor-memory-access copies for regions inside the grid, plain
+ * loads for regions across the periodic boundary), the next tile's copies in
+ * flight while one is evaluated; 4 = markers of dense home tiles as in 3,
+ * the others in chunks.  Every form sums in the same order: identical
+ * results. */
 int ibx_plan_set_interp_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_interp_kernel(const ibx_plan* plan);
 /* How ibx_plan_step orders spread and interpolation after the binning (no
@@ -296,6 +303,12 @@ int ibx_plan_get_step_mode(const ibx_plan* plan);
  * merges.  Default 32.  Takes effect at the next ibx_plan_bin. */
 int ibx_plan_set_unit_cap(ibx_plan* plan, int cap);
 int ibx_plan_get_unit_cap(const ibx_plan* plan);
+/* Number of the plan's problems whose interpolation sources the staged
+ * forms (3, 4) load by tensor copies: the x extent a multiple of 4 values,
+ * every grid dimension at least the staged box, 16-byte aligned arrays, and
+ * a driver that encodes tensor maps.  The others are staged with plain
+ * loads.  No reference counterpart. */
+int ibx_plan_tma_problems(const ibx_plan* plan);
 /* Bytes of device scratch the plan holds. */
 long long ibx_plan_scratch_bytes(const ibx_plan* plan);
 int ibx_plan_destroy(ibx_plan* plan);

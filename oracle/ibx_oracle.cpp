@@ -14,6 +14,7 @@
 #include <cstring>
 #include <random>
 #include <string>
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -788,7 +789,18 @@ ibxo_mt19937_uniform(unsigned seed, int n, double a, double b, double* out)
 } // extern "C"
 
 // ---------------------------------------------------------------------------
-// CPU baseline: per-patch LEInteractor calls on slab patches, one thread each.
+// CPU baseline: the reference's per-patch flow (LDataManager::spread /
+// interp, src/IB/LDataManager.cpp:552-811, one LEInteractor call per patch
+// and field) over box patches of a periodic domain.  The boxes come from a
+// recursive bisection of the domain by marker workload, as a load balancer
+// with per-marker workload estimates would cut a level (many boxes per
+// thread, the densest regions in the smallest boxes); a pool of threads takes
+// the boxes largest first, like ranks each working through their patches.
+// Every patch spreads its ghost-box markers (with periodic shifts) into
+// zeroed patch data and adds its own faces into the global field, then fills
+// the ghosts of its copy of u from the global field and interpolates at its
+// interior markers.  The copies between global and patch arrays run row by
+// row (contiguous along x, with the periodic wrap resolved per row).
 // ---------------------------------------------------------------------------
 namespace
 {
@@ -797,69 +809,175 @@ struct CpuPatch
     ibxo_patch P;
     std::vector<int> sp_idx, in_idx;
     std::vector<double> sp_shift, in_shift;
-    std::vector<double> f_loc[3], u_loc[3];
-    int lo[3][3], hi[3][3]; // ghosted side box per axis
+    int lo[3][3], hi[3][3]; // side box per axis (cell box with upper(axis) + 1)
+    long long work;         // ghost-box markers + cells / 8: the scheduling order
 };
 
 struct CpuPlan
 {
-    int dim, N[3], kernel, n_markers, gcw;
+    int dim, N[3], kernel, n_markers, gcw, n_threads;
     const double* X;
-    std::vector<CpuPatch> patches;
+    std::vector<CpuPatch> patches; // largest work first
+    long long max_ghosted;         // largest ghosted side array over patches and axes
 };
 
-inline long long
-wrap_off(int dim, const int* N, const int* i)
+struct Box
 {
-    long long o = 0;
-    for (int d = dim - 1; d >= 0; --d) o = o * N[d] + (((i[d] % N[d]) + N[d]) % N[d]);
-    return o;
-}
+    int lo[3], hi[3];
+};
 
+// Recursive bisection of `box` into n leaves: the longest side is cut where
+// the workload (markers + cells / 8) on the lower side reaches its share;
+// no side shorter than min_edge.
 void
-cpu_patch_step(const CpuPlan& plan, CpuPatch& cp, const double* F, double* f, const double* u, double* U)
+bisect(const CpuPlan& plan, const Box& box, const std::vector<int>& cell, std::vector<int> members, int n,
+       int min_edge, std::vector<Box>& out)
 {
     const int dim = plan.dim;
-    long long vol = 1;
-    for (int d = 0; d < dim; ++d) vol *= plan.N[d];
+    int ax = 0;
+    for (int d = 1; d < dim; ++d)
+        if (box.hi[d] - box.lo[d] > box.hi[ax] - box.lo[ax]) ax = d;
+    const int len = box.hi[ax] - box.lo[ax] + 1;
+    if (n <= 1 || len < 2 * min_edge)
+    {
+        out.push_back(box);
+        return;
+    }
+    long long cross = 1;
+    for (int d = 0; d < dim; ++d)
+        if (d != ax) cross *= box.hi[d] - box.lo[d] + 1;
+    std::vector<double> w(len, cross / 8.0);
+    for (int s : members) w[cell[(size_t)dim * s + ax] - box.lo[ax]] += 1.0;
+    double total = 0.0;
+    for (double v : w) total += v;
+    const int n_lo = n / 2;
+    const double target = total * n_lo / n;
+    double acc = 0.0;
+    int cut = box.lo[ax] + min_edge; // first cell of the upper part
+    for (int i = 0; i < len; ++i)
+    {
+        acc += w[i];
+        if (acc >= target)
+        {
+            cut = box.lo[ax] + i + 1;
+            break;
+        }
+    }
+    cut = std::max(cut, box.lo[ax] + min_edge);
+    cut = std::min(cut, box.hi[ax] + 1 - min_edge);
+    Box a = box, b = box;
+    a.hi[ax] = cut - 1;
+    b.lo[ax] = cut;
+    std::vector<int> ma, mb;
+    for (int s : members) (cell[(size_t)dim * s + ax] < cut ? ma : mb).push_back(s);
+    members.clear();
+    members.shrink_to_fit();
+    bisect(plan, a, cell, std::move(ma), n_lo, min_edge, out);
+    bisect(plan, b, cell, std::move(mb), n - n_lo, min_edge, out);
+}
+
+// Markers whose cell lies in the box grown by g (periodic images along every
+// dimension), with the periodic shift rule of LIndexSetData.cpp:83-100 as
+// ibxo_cache_local_indices states it.
+void
+select_markers(const CpuPlan& plan, const ibxo_patch& P, const std::vector<int>& cell, int g, std::vector<int>& idx,
+               std::vector<double>& shift)
+{
+    const int dim = plan.dim;
+    idx.clear();
+    shift.clear();
+    for (int s = 0; s < plan.n_markers; ++s)
+    {
+        int kk[3][3], nk[3] = { 0, 0, 0 };
+        bool any = true;
+        for (int d = 0; d < dim && any; ++d)
+        {
+            const int c = cell[(size_t)dim * s + d];
+            for (int k = -1; k <= 1; ++k)
+            {
+                const int i = c + k * plan.N[d];
+                if (i < P.ilower[d] - g || i > P.iupper[d] + g) continue;
+                const int off = (P.touches_periodic_lower[d] && i < P.ilower[d])   ? -1
+                                : (P.touches_periodic_upper[d] && i > P.iupper[d]) ? 1
+                                                                                   : 0;
+                if (off == k) kk[d][nk[d]++] = k;
+            }
+            any = nk[d] > 0;
+        }
+        if (!any) continue;
+        const int nimg = nk[0] * nk[1] * (dim == 3 ? nk[2] : 1);
+        for (int m = 0; m < nimg; ++m)
+        {
+            const int j[3] = { m % nk[0], (m / nk[0]) % nk[1], dim == 3 ? m / (nk[0] * nk[1]) : 0 };
+            idx.push_back(s);
+            for (int d = 0; d < dim; ++d) shift.push_back(kk[d][j[d]] * plan.N[d] * P.dx[d]);
+        }
+    }
+}
+
+struct CpuScratch
+{
+    std::vector<double> f_loc[3], u_loc[3];
+};
+
+void
+cpu_patch_step(const CpuPlan& plan, const CpuPatch& cp, CpuScratch& sc, const double* F, double* f, const double* u,
+               double* U)
+{
+    const int dim = plan.dim;
+    const long long n0 = plan.N[0], n01 = (long long)plan.N[0] * plan.N[1];
+    const long long vol = n01 * (dim == 3 ? plan.N[2] : 1);
     ibxo_patch_data q;
     q.depth = 1;
     q.centering = 1;
     for (int d = 0; d < 3; ++d) q.gcw[d] = d < dim ? plan.gcw : 0;
-    // Spread into zeroed patch data, then add the patch's own faces into f.
+    ArrayGeom G[3];
     for (int a = 0; a < dim; ++a)
     {
-        std::fill(cp.f_loc[a].begin(), cp.f_loc[a].end(), 0.0);
-        q.ptr[a] = cp.f_loc[a].data();
+        G[a] = make_geom(dim, cp.lo[a], cp.hi[a], q.gcw);
+        std::fill(sc.f_loc[a].begin(), sc.f_loc[a].begin() + G[a].vol, 0.0);
+        q.ptr[a] = sc.f_loc[a].data();
     }
+    // Spread into zeroed patch data, then add the patch's own faces into f
+    // (cells ilower..iupper along every axis: face iupper + 1 of a side axis
+    // belongs to the next patch).
     ibxo_lei_spread_idx(&q, F, dim, plan.X, cp.sp_idx.data(), cp.sp_shift.data(), (int)cp.sp_idx.size(), &cp.P,
                         plan.kernel);
+    const int z0 = dim == 3 ? cp.P.ilower[2] : 0, z1 = dim == 3 ? cp.P.iupper[2] : 0;
+    const int x0 = cp.P.ilower[0], nx = cp.P.iupper[0] - x0 + 1;
+    for (int a = 0; a < dim; ++a)
+        for (int z = z0; z <= z1; ++z)
+            for (int y = cp.P.ilower[1]; y <= cp.P.iupper[1]; ++y)
+            {
+                const int i[3] = { x0, y, z };
+                const double* src = sc.f_loc[a].data() + G[a].off(i, 0);
+                double* dst = f + vol * a + z * n01 + y * n0 + x0;
+                for (int k = 0; k < nx; ++k) dst[k] += src[k];
+            }
+    // Ghost fill of u (periodic copy of the global field) row by row, then
+    // interpolation at the interior markers.
     for (int a = 0; a < dim; ++a)
     {
-        const ArrayGeom G = make_geom(dim, cp.lo[a], cp.hi[a], q.gcw);
-        int i[3] = { 0, 0, 0 };
-        const int z0 = dim == 3 ? cp.P.ilower[2] : 0, z1 = dim == 3 ? cp.P.iupper[2] : 0;
-        for (i[2] = z0; i[2] <= z1; ++i[2])
-            for (i[1] = cp.P.ilower[1]; i[1] <= cp.P.iupper[1]; ++i[1])
-                for (i[0] = cp.P.ilower[0]; i[0] <= cp.P.iupper[0]; ++i[0])
-                    f[vol * a + wrap_off(dim, plan.N, i)] += cp.f_loc[a][G.off(i, 0)];
-    }
-    // Ghost fill of u (periodic copy) and interpolation of interior markers.
-    for (int a = 0; a < dim; ++a)
-    {
-        const ArrayGeom G = make_geom(dim, cp.lo[a], cp.hi[a], q.gcw);
-        int i[3] = { 0, 0, 0 };
-        const int n2 = dim == 3 ? G.n[2] : 1;
+        const ArrayGeom& g = G[a];
+        const int n2 = dim == 3 ? g.n[2] : 1;
         for (int k2 = 0; k2 < n2; ++k2)
-            for (int k1 = 0; k1 < G.n[1]; ++k1)
-                for (int k0 = 0; k0 < G.n[0]; ++k0)
+        {
+            int jz = dim == 3 ? g.glo[2] + k2 : 0;
+            if (dim == 3) jz = ((jz % plan.N[2]) + plan.N[2]) % plan.N[2];
+            for (int k1 = 0; k1 < g.n[1]; ++k1)
+            {
+                const int jy = (((g.glo[1] + k1) % plan.N[1]) + plan.N[1]) % plan.N[1];
+                const double* row = u + vol * a + jz * n01 + jy * n0;
+                double* dst = sc.u_loc[a].data() + ((long long)k2 * g.n[1] + k1) * g.n[0];
+                int jx = ((g.glo[0] % plan.N[0]) + plan.N[0]) % plan.N[0];
+                for (int k0 = 0; k0 < g.n[0]; ++k0)
                 {
-                    i[0] = G.glo[0] + k0;
-                    i[1] = G.glo[1] + k1;
-                    i[2] = G.glo[2] + k2;
-                    cp.u_loc[a][G.off(i, 0)] = u[vol * a + wrap_off(dim, plan.N, i)];
+                    dst[k0] = row[jx];
+                    if (++jx == plan.N[0]) jx = 0;
                 }
-        q.ptr[a] = cp.u_loc[a].data();
+            }
+        }
+        q.ptr[a] = sc.u_loc[a].data();
     }
     ibxo_lei_interpolate_idx(U, dim, plan.X, cp.in_idx.data(), cp.in_shift.data(), (int)cp.in_idx.size(), &q, &cp.P,
                              plan.kernel);
@@ -869,20 +987,44 @@ cpu_patch_step(const CpuPlan& plan, CpuPatch& cp, const double* F, double* f, co
 extern "C" {
 
 void*
-ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const double* X, int n_patches)
+ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const double* X, int n_threads, int n_boxes)
 {
-    if ((dim != 2 && dim != 3) || !valid_kernel(kernel) || n_patches < 1) return nullptr;
+    if ((dim != 2 && dim != 3) || !valid_kernel(kernel) || n_threads < 1 || n_boxes < 1) return nullptr;
     CpuPlan* plan = new CpuPlan;
     plan->dim = dim;
     plan->kernel = kernel;
     plan->n_markers = n_markers;
+    plan->n_threads = n_threads;
     plan->X = X;
     plan->gcw = ibxo_min_ghost_width(kernel);
     for (int d = 0; d < 3; ++d) plan->N[d] = d < dim ? N[d] : 1;
-    const int split = dim - 1;
-    n_patches = std::min(n_patches, plan->N[split]);
-    plan->patches.resize(n_patches);
-    auto build_patch = [plan, dim, split, n_patches, n_markers, X](int p) {
+    // Cell of every marker on the domain (getCellIndex, unit domain).
+    double xl[3] = { 0, 0, 0 }, xu[3] = { 1, 1, 1 }, dx[3] = { 1, 1, 1 };
+    int il[3] = { 0, 0, 0 }, iu[3] = { 0, 0, 0 };
+    for (int d = 0; d < dim; ++d)
+    {
+        dx[d] = 1.0 / plan->N[d];
+        iu[d] = plan->N[d] - 1;
+    }
+    std::vector<int> cell((size_t)dim * n_markers);
+    for (int s = 0; s < n_markers; ++s)
+    {
+        int c[3];
+        ibxo_get_cell_index(dim, &X[(size_t)dim * s], xl, xu, dx, il, iu, c);
+        for (int d = 0; d < dim; ++d) cell[(size_t)dim * s + d] = ((c[d] % plan->N[d]) + plan->N[d]) % plan->N[d];
+    }
+    Box dom;
+    for (int d = 0; d < 3; ++d)
+    {
+        dom.lo[d] = 0;
+        dom.hi[d] = plan->N[d] - 1;
+    }
+    std::vector<int> all(n_markers);
+    for (int s = 0; s < n_markers; ++s) all[s] = s;
+    std::vector<Box> boxes;
+    bisect(*plan, dom, cell, std::move(all), n_boxes, std::max(4, plan->gcw), boxes);
+    plan->patches.resize(boxes.size());
+    auto build_patch = [plan, dim, &boxes, &cell](size_t p) {
         CpuPatch& cp = plan->patches[p];
         ibxo_patch& P = cp.P;
         std::memset(&P, 0, sizeof(P));
@@ -890,48 +1032,46 @@ ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const dou
         for (int d = 0; d < dim; ++d)
         {
             P.dx[d] = 1.0 / plan->N[d];
-            P.ilower[d] = 0;
-            P.iupper[d] = plan->N[d] - 1;
-        }
-        P.ilower[split] = (int)((long long)plan->N[split] * p / n_patches);
-        P.iupper[split] = (int)((long long)plan->N[split] * (p + 1) / n_patches) - 1;
-        for (int d = 0; d < dim; ++d)
-        {
+            P.ilower[d] = boxes[p].lo[d];
+            P.iupper[d] = boxes[p].hi[d];
             P.x_lower[d] = P.ilower[d] * P.dx[d];
             P.x_upper[d] = (P.iupper[d] + 1) * P.dx[d];
             P.touches_periodic_lower[d] = P.ilower[d] == 0;
             P.touches_periodic_upper[d] = P.iupper[d] == plan->N[d] - 1;
         }
-        int gw[3] = { plan->gcw, plan->gcw, plan->gcw };
-        const int cap = 8 * std::max(n_markers, 1);
-        std::vector<int> idx(cap);
-        std::vector<double> sh((size_t)cap * dim);
-        int n = ibxo_cache_local_indices(&P, plan->N, gw, 1, X, n_markers, cap, idx.data(), sh.data());
-        n = std::min(n, cap);
-        cp.sp_idx.assign(idx.begin(), idx.begin() + n);
-        cp.sp_shift.assign(sh.begin(), sh.begin() + (size_t)n * dim);
-        n = ibxo_cache_local_indices(&P, plan->N, gw, 0, X, n_markers, cap, idx.data(), sh.data());
-        n = std::min(n, cap);
-        cp.in_idx.assign(idx.begin(), idx.begin() + n);
-        cp.in_shift.assign(sh.begin(), sh.begin() + (size_t)n * dim);
+        select_markers(*plan, P, cell, plan->gcw, cp.sp_idx, cp.sp_shift);
+        select_markers(*plan, P, cell, 0, cp.in_idx, cp.in_shift);
+        long long cells = 1;
         for (int a = 0; a < dim; ++a)
-        {
-            long long vol = 1;
             for (int d = 0; d < dim; ++d)
             {
                 cp.lo[a][d] = P.ilower[d];
                 cp.hi[a][d] = P.iupper[d] + (d == a ? 1 : 0);
-                vol *= cp.hi[a][d] - cp.lo[a][d] + 1 + 2 * plan->gcw;
             }
-            cp.f_loc[a].assign(vol, 0.0);
-            cp.u_loc[a].assign(vol, 0.0);
-        }
+        for (int d = 0; d < dim; ++d) cells *= P.iupper[d] - P.ilower[d] + 1;
+        cp.work = (long long)cp.sp_idx.size() + cells / 8;
     };
     // Patches are independent: build their index sets concurrently.
-    std::vector<std::thread> threads;
-    for (int p = 1; p < n_patches; ++p) threads.emplace_back(build_patch, p);
-    build_patch(0);
-    for (auto& t : threads) t.join();
+    {
+        std::atomic<size_t> next(0);
+        auto worker = [&]() {
+            for (size_t p = next++; p < boxes.size(); p = next++) build_patch(p);
+        };
+        std::vector<std::thread> threads;
+        for (int t = 1; t < n_threads; ++t) threads.emplace_back(worker);
+        worker();
+        for (auto& t : threads) t.join();
+    }
+    std::sort(plan->patches.begin(), plan->patches.end(),
+              [](const CpuPatch& a, const CpuPatch& b) { return a.work > b.work; });
+    plan->max_ghosted = 0;
+    for (const CpuPatch& cp : plan->patches)
+        for (int a = 0; a < dim; ++a)
+        {
+            long long v = 1;
+            for (int d = 0; d < dim; ++d) v *= cp.hi[a][d] - cp.lo[a][d] + 1 + 2 * plan->gcw;
+            plan->max_ghosted = std::max(plan->max_ghosted, v);
+        }
     return plan;
 }
 
@@ -940,12 +1080,29 @@ ibxo_cpu_plan_step(void* handle, const double* F, double* f, const double* u, do
 {
     CpuPlan* plan = static_cast<CpuPlan*>(handle);
     if (!plan) return IBXO_E_ARG;
+    std::atomic<size_t> next(0);
+    auto worker = [&]() {
+        CpuScratch sc;
+        for (int a = 0; a < plan->dim; ++a)
+        {
+            sc.f_loc[a].resize(plan->max_ghosted);
+            sc.u_loc[a].resize(plan->max_ghosted);
+        }
+        for (size_t p = next++; p < plan->patches.size(); p = next++)
+            cpu_patch_step(*plan, plan->patches[p], sc, F, f, u, U);
+    };
     std::vector<std::thread> threads;
-    for (size_t p = 1; p < plan->patches.size(); ++p)
-        threads.emplace_back(cpu_patch_step, std::cref(*plan), std::ref(plan->patches[p]), F, f, u, U);
-    cpu_patch_step(*plan, plan->patches[0], F, f, u, U);
+    for (int t = 1; t < plan->n_threads; ++t) threads.emplace_back(worker);
+    worker();
     for (auto& t : threads) t.join();
     return IBXO_OK;
+}
+
+int
+ibxo_cpu_plan_patches(void* handle)
+{
+    CpuPlan* plan = static_cast<CpuPlan*>(handle);
+    return plan ? (int)plan->patches.size() : -1;
 }
 
 void

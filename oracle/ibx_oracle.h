@@ -151,18 +151,23 @@ int ibxo_fill_periodic_ghosts(const ibxo_patch_data* q, const ibxo_patch* patch)
 void ibxo_mt19937_uniform(unsigned seed, int n, double a, double b, double* out);
 
 /* CPU baseline (the reference's per-patch CPU path, multi-threaded the way
- * IBAMR runs one MPI rank per patch).  One periodic single-level problem on
- * [0,1)^dim with N[d] cells is split into n_patches slabs along the last
- * axis.  The plan caches each patch's LIndexSetData lists (ghost-box markers
- * with periodic shifts for spreading, interior markers for interpolation),
- * as LDataManager does between regrids.  A step then, for every patch on its
- * own thread: zeroes ghosted side arrays, spreads (LEI:3627-3714), adds the
- * patch interior into f; copies u into ghosted side arrays (the periodic
- * ghost fill) and interpolates (LEI:2402-2489) into U.
- * f and u are compact periodic side arrays: dim arrays of prod(N) doubles,
- * x fastest, face i of axis a at x_lower + i*dx (face N == face 0).
- * F and U hold dim values per marker.  The plan keeps pointers to X. */
-void* ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const double* X, int n_patches);
+ * IBAMR runs ranks that each work through their patches).  One periodic
+ * single-level problem on [0,1)^dim with N[d] cells is cut into n_boxes box
+ * patches by recursive bisection on marker workload (markers + cells / 8
+ * per cell, longest side first, no side below max(4, ghost width)).  The
+ * plan caches each patch's LIndexSetData lists (ghost-box markers with
+ * periodic shifts for spreading, interior markers for interpolation), as
+ * LDataManager does between regrids.  A step then runs the patches on
+ * n_threads threads, largest first: per patch it zeroes ghosted side arrays,
+ * spreads (LEI:3627-3714), adds the patch interior into f; copies u into
+ * ghosted side arrays (the periodic ghost fill) and interpolates
+ * (LEI:2402-2489) into U.  f and u are compact periodic side arrays: dim
+ * arrays of prod(N) doubles, x fastest, face i of axis a at x_lower + i*dx
+ * (face N == face 0).  F and U hold dim values per marker.  The plan keeps
+ * pointers to X.  ibxo_cpu_plan_patches: number of patches. */
+void* ibxo_cpu_plan_create(int dim, const int* N, int kernel, int n_markers, const double* X, int n_threads,
+                           int n_boxes);
+int ibxo_cpu_plan_patches(void* plan);
 int ibxo_cpu_plan_step(void* plan, const double* F, double* f, const double* u, double* U);
 void ibxo_cpu_plan_destroy(void* plan);
 

@@ -81,8 +81,10 @@ def lib():
                                                           _ip]
         L.ibxo_fill_periodic_ghosts.argtypes = [ctypes.POINTER(PatchData), ctypes.POINTER(Patch)]
         L.ibxo_mt19937_uniform.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
-        L.ibxo_cpu_plan_create.argtypes = [ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]
+        L.ibxo_cpu_plan_create.argtypes = [ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int,
+                                           ctypes.c_int]
         L.ibxo_cpu_plan_create.restype = ctypes.c_void_p
+        L.ibxo_cpu_plan_patches.argtypes = [ctypes.c_void_p]
         L.ibxo_cpu_plan_step.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
         L.ibxo_cpu_plan_destroy.argtypes = [ctypes.c_void_p]
         _lib = L
@@ -307,15 +309,21 @@ def periodic_side_problem(dim, N, kernel, X, F=None, u=None):
 
 
 class CpuPlan:
-    """Multi-threaded per-patch CPU baseline (see ibxo_cpu_plan_create)."""
+    """Multi-threaded per-patch CPU baseline (see ibxo_cpu_plan_create):
+    ``threads`` host threads working through ``boxes`` box patches (default:
+    one patch for one thread, else four patches per thread)."""
 
-    def __init__(self, dim, N, kernel, X, n_patches):
+    def __init__(self, dim, N, kernel, X, threads=1, boxes=None):
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.dim = dim
+        if boxes is None:
+            boxes = 1 if threads == 1 else 4 * threads
         self.h = lib().ibxo_cpu_plan_create(dim, ivec(N), kernel_id(kernel), self.X.size // dim, dptr(self.X),
-                                            int(n_patches))
+                                            int(threads), int(boxes))
         if not self.h:
             raise ValueError("bad CPU plan arguments")
+        self.threads = int(threads)
+        self.patches = lib().ibxo_cpu_plan_patches(self.h)
 
     def step(self, F, f, u, U):
         rc = lib().ibxo_cpu_plan_step(self.h, dptr(F), dptr(f), dptr(u), dptr(U))

@@ -361,7 +361,7 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
 
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("step_mode", [0, 1])
-@pytest.mark.parametrize("interp_form", [0, 1, 2])
+@pytest.mark.parametrize("interp_form", [0, 1, 2, 3, 4])
 def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_form, step_mode):
     """ibx_plan_step (spread and interpolation on two streams, or one after
     the other; the marker-order interpolation forked before the counting
@@ -422,16 +422,22 @@ def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_sha
     pi.close()
 
 
+# Grids (52 x 35), (40 x 36 x 32) and (64 x 48) hold tiles whose staged
+# interpolation region lies inside the grid (tensor copies); 27 x 20 x 34 is
+# not a multiple of 4 along x (plain loads only); 32 x 20 x 18 has no
+# interior region for 3D stencils.
 @pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
-@pytest.mark.parametrize("dim,N", [(2, [52, 35]), (3, [27, 20, 34]), (3, [32, 20, 18])])
+@pytest.mark.parametrize("dim,N", [(2, [52, 35]), (2, [64, 48]), (3, [27, 20, 34]), (3, [32, 20, 18]),
+                                   (3, [40, 36, 32])])
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
 @pytest.mark.parametrize("dense_min", [0, 8])
 def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, tile_shape, dense_min):
     """Every interpolation form (chunks in home order, dense-homed markers per
-    home unit, chunks in marker order) sums in the same order: bit-identical
-    results (every tile dense, then a mix), all within the bar of the
-    oracle."""
+    home unit, chunks in marker order, regions staged in shared memory for
+    every marker or for the dense-homed ones) sums in the same order:
+    bit-identical results (every tile dense, then a mix), all within the bar
+    of the oracle."""
     rng = np.random.default_rng(91 + N[0] + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     n = 2000
     X = seam_markers(rng, n, dim)
@@ -440,16 +446,45 @@ def test_interp_forms_identical(ibx, oracle, kernel, dim, N, centering, depth, t
     u = rng.standard_normal([ncomp] + list(N)[::-1])
     f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
     got = []
-    for form in (1, 2, 0):
+    for form in (1, 2, 3, 4, 0):
         f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=dense_min,
                                 tile_shape=tile_shape, interp_kernel=form)
         assert pi.interp_kernel == form
+        assert pi.status() == ibx.OK
         assert cases.rel_err(U, U_ref) <= MIXED_TOL
         got.append(U)
         ps.close()
         pi.close()
     for g in got[:-1]:
         assert np.array_equal(g, got[-1])
+
+
+@pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "BSPLINE_4"])
+@pytest.mark.parametrize("dim,N,tma", [(3, [64, 48, 40], 1), (3, [62, 48, 40], 0), (2, [96, 80], 1)])
+def test_staged_interpolation_uses_tensor_copies(ibx, oracle, kernel, dim, N, tma):
+    """The staged interpolation form loads interior regions by tensor copies
+    where the layout allows (x extent a multiple of 4 values) and by plain
+    loads otherwise; both give the chunked form's values bit for bit, on
+    clustered (dense) and uniform (sparse) markers, within the bar of the
+    oracle."""
+    rng = np.random.default_rng(17 + N[0] + 3 * KERNEL_NAMES.index(kernel))
+    n = 6000
+    X = np.concatenate([0.5 + 0.04 * rng.standard_normal((n // 2, dim)),
+                        rng.uniform(0.0, 1.0, size=(n - n // 2, dim))])
+    X = np.mod(X, 1.0).reshape(-1)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=1)
+    got = []
+    for form in (3, 0):
+        f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, 1, 1, interp_kernel=form)
+        assert pi.tma_problems == tma
+        assert pi.status() == ibx.OK
+        assert cases.rel_err(U, U_ref) <= MIXED_TOL
+        got.append(U)
+        ps.close()
+        pi.close()
+    assert np.array_equal(got[0], got[1])
 
 
 @pytest.mark.parametrize("cap", [1, 5, 32])
