@@ -208,8 +208,15 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
     const int group = warp * US::GPW + lane / ZS;
     const int n_groups = (INTERP_THREADS / 32) * US::GPW;
     const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
-    for (int item = blockIdx.x; item < n_items; item += gridDim.x)
+    __shared__ int s_item;
+    // items are taken from a counter (no tail from CTAs resident late)
+    for (;;)
     {
+        __syncthreads(); // the previous item's readers of s_item and s_order are done
+        if (threadIdx.x == 0) s_item = atomicAdd(&D.work[2], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items) break;
         const int t = D.item_tile[item];
         const int k = item - D.items[t];
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
@@ -222,7 +229,6 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
         // the item's units, longest first, as in the dense spread
         __shared__ int s_order[256];
         __shared__ int s_start[33];
-        __syncthreads(); // the previous item's readers of s_order are done
         if (threadIdx.x < 33) s_start[threadIdx.x] = 0;
         __syncthreads();
         for (int i = threadIdx.x; i < nu; i += blockDim.x)
@@ -611,6 +617,7 @@ launch_interp_k(const DevPlan& D, cudaStream_t s)
     const bool units = D.interp_form == 1 && UnitSplit<DIM, W>::NC <= 64;
     if (units)
     {
+        if (cudaMemsetAsync(D.work + 2, 0, sizeof(int), s) != cudaSuccess) return IBX_E_CUDA;
         int dev = 0, sms = 152, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -134,6 +134,7 @@ carve_plan(const PlanSizes& z, char* b, DevPlan& D)
     D.tile_shape = z.tile_shape;
     D.dense_blocks_per_sm = 2;
     D.status = reinterpret_cast<int*>(b + c.o_status);
+    D.work = D.status + 1;
     D.tmaps = reinterpret_cast<const CUtensorMap*>(b + c.o_tmaps);
     c.scan_tmp = reinterpret_cast<int*>(b + o_scan);
     return c;
@@ -150,10 +151,13 @@ struct ibx_plan
     void* dmem;
     size_t dbytes;
     int* scan_tmp;
-    // ibx_plan_step: interpolation forks onto `side` after the binning
-    // (step_mode 1) or follows the spread on the caller's stream (0)
-    cudaStream_t side;
-    cudaEvent_t ev_fork, ev_join;
+    // ibx_plan_step: after the binning, the spread forks onto `spread_s`
+    // (greatest stream priority: it is the longer phase) and the
+    // interpolation onto `side` (least priority), both joined back into the
+    // caller's stream (step_mode 1); or the spread then the interpolation on
+    // the caller's stream (0)
+    cudaStream_t side, spread_s;
+    cudaEvent_t ev_fork, ev_join, ev_join2;
     int step_mode;
     int n_tma; // problems whose interpolation sources have tensor maps
 };
@@ -322,9 +326,13 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     }
     plan->scan_tmp = c.scan_tmp;
     plan->step_mode = 1;
-    if (cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking) != cudaSuccess ||
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&plan->side, cudaStreamNonBlocking, least) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&plan->spread_s, cudaStreamNonBlocking, greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_join2, cudaEventDisableTiming) != cudaSuccess)
     {
         cudaFree(dmem);
         delete plan;
@@ -365,15 +373,20 @@ ibx_plan_step(ibx_plan* plan, void* stream)
         rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
         return rc ? rc : launch_interp(plan->dim, plan->kernel, plan->D, s);
     }
-    // spread (stream) and interpolation (side) read the same records and
-    // write different arrays: they overlap on the device
+    // spread and interpolation read the same records and write different
+    // arrays: they overlap on the device, the spread's blocks dispatched first
     if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
         cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
         return IBX_E_CUDA;
+    if (early && cudaEventRecord(plan->ev_join2, s) != cudaSuccess) return IBX_E_CUDA; // the whole binning
+    if (cudaStreamWaitEvent(plan->spread_s, early ? plan->ev_join2 : plan->ev_fork, 0) != cudaSuccess)
+        return IBX_E_CUDA;
     rc = launch_interp(plan->dim, plan->kernel, plan->D, plan->side);
-    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
-    // join even after a failed launch, so that the side stream is never left forked
-    if (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess || cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess)
+    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, plan->spread_s);
+    // join even after a failed launch, so that no stream of the plan is left forked
+    if (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
+        cudaEventRecord(plan->ev_join2, plan->spread_s) != cudaSuccess ||
+        cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess || cudaStreamWaitEvent(s, plan->ev_join2, 0) != cudaSuccess)
         return IBX_E_CUDA;
     return rc ? rc : rs;
 }
@@ -452,7 +465,7 @@ ibx_plan_set_tuning(ibx_plan* plan, int item_units, int dense_min, int dense_blo
 int
 ibx_plan_set_visit_kernel(ibx_plan* plan, int form)
 {
-    if (!plan || form < 0 || form > 2) return IBX_E_ARG;
+    if (!plan || form < 0 || form > 3) return IBX_E_ARG;
     plan->D.visit_kernel = form;
     return IBX_OK;
 }
@@ -546,9 +559,12 @@ ibx_plan_destroy(ibx_plan* plan)
 {
     if (!plan) return IBX_OK;
     cudaStreamSynchronize(plan->side);
+    cudaStreamSynchronize(plan->spread_s);
     cudaStreamDestroy(plan->side);
+    cudaStreamDestroy(plan->spread_s);
     cudaEventDestroy(plan->ev_fork);
     cudaEventDestroy(plan->ev_join);
+    cudaEventDestroy(plan->ev_join2);
     const cudaError_t e = cudaFree(plan->dmem);
     delete plan;
     return e == cudaSuccess ? IBX_OK : IBX_E_CUDA;

@@ -155,6 +155,8 @@ struct DevPlan
     int unit_cap;     // most markers per home unit (1..32)
     int tile_shape;   // TileT shape id of every tile of the plan
     int* status;      // error word: bit 0 non-finite position, bit 1 visit overflow, bit 2 wait timeout
+    int* work;        // [3] work counters (dense spread items, visited tiles, dense interpolation items),
+                      // zeroed before each launch that takes from them
     // Tensor maps of the interpolation sources, 3 per problem (one per
     // component), valid where the problem's tma flag is set.
     const CUtensorMap* tmaps;

@@ -147,9 +147,16 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
     constexpr int CSTR = RG::CSTR;
     constexpr int NF = RG::NF;
     extern __shared__ float sm[]; // [ncomp][hi, lo][PAD], components CSTR apart
-    const int n_items = D.items[D.n_tiles];
-    for (int item = blockIdx.x; item < n_items && item < D.n_item_cap; item += gridDim.x)
+    __shared__ int s_item;
+    const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
+    // Work items are taken from a counter, so that CTAs that become resident
+    // late (beside other kernels, or in a second wave) do not leave a tail.
+    for (;;)
     {
+        if (threadIdx.x == 0) s_item = atomicAdd(&D.work[0], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items) break;
         const int t = D.item_tile[item];
         const int k = item - D.items[t];
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
@@ -746,9 +753,11 @@ struct GatherOccupancy
     static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 4;
 };
 
-template <int DIM, int K, int SH>
-__global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::value)
-    spread_visits_gather(const DevPlan D)
+// OCC: CTAs per SM the register budget is cut for (form 2: GatherOccupancy,
+// 64 registers for 3D tiles of 8^3, a few values spilled; form 3: one CTA per
+// SM fewer, no spills).
+template <int DIM, int K, int SH, int OCC>
+__global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
     using T = TileT<DIM, SH>;
@@ -767,8 +776,13 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
     const int y0 = r0 % T::E1;
     const int z0 = r0 / T::E1;
     static_assert(NR == 1 || (NR == 2 && T::E1 % 2 == 0), "a lane's rows share their plane");
-    for (int t = blockIdx.x * GATHER_WARPS + warp; t < D.n_tiles; t += gridDim.x * GATHER_WARPS)
+    // each warp takes its next tile from a counter (no tail from late CTAs)
+    for (;;)
     {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&D.work[1], 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= D.n_tiles) break;
         const int vbeg = D.vcount[t];
         const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
         if (vend <= vbeg) continue;
@@ -913,6 +927,27 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, GatherOccupancy<DIM, SH>::v
 
 namespace
 {
+template <int DIM, int K, int SH, int OCC>
+int
+launch_gather(const DevPlan& D, cudaStream_t s, int sms)
+{
+    using GL = GatherLayout<DIM, SH>;
+    const size_t smem_g = sizeof(float) * 32 * GL::SS * GATHER_WARPS;
+    if (smem_g > 48 * 1024 &&
+        cudaFuncSetAttribute(spread_visits_gather<DIM, K, SH, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_g) != cudaSuccess)
+        return IBX_E_CUDA;
+    int per_sm_g = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_g, spread_visits_gather<DIM, K, SH, OCC>, 32 * GATHER_WARPS,
+                                                  smem_g);
+    if (per_sm_g < 1) per_sm_g = 1;
+    const unsigned need_g = (unsigned)((D.n_tiles + GATHER_WARPS - 1) / GATHER_WARPS);
+    const unsigned blocks_g = need_g < (unsigned)(per_sm_g * sms) ? need_g : (unsigned)(per_sm_g * sms);
+    spread_visits_gather<DIM, K, SH, OCC><<<blocks_g, 32 * GATHER_WARPS, smem_g, s>>>(D);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
 template <int DIM, int K, int SH>
 int
 launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
@@ -931,23 +966,12 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
         note_launches(1);
         if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
     }
-    if (D.visit_kernel == 2)
+    if (D.visit_kernel == 2 || D.visit_kernel == 3)
     {
-        using GL = GatherLayout<DIM, SH>;
-        const size_t smem_g = sizeof(float) * 32 * GL::SS * GATHER_WARPS;
-        if (smem_g > 48 * 1024 &&
-            cudaFuncSetAttribute(spread_visits_gather<DIM, K, SH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_g) != cudaSuccess)
-            return IBX_E_CUDA;
-        int per_sm_g = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_g, spread_visits_gather<DIM, K, SH>,
-                                                      32 * GATHER_WARPS, smem_g);
-        if (per_sm_g < 1) per_sm_g = 1;
-        const unsigned need_g = (unsigned)((D.n_tiles + GATHER_WARPS - 1) / GATHER_WARPS);
-        const unsigned blocks_g = need_g < (unsigned)(per_sm_g * sms) ? need_g : (unsigned)(per_sm_g * sms);
-        spread_visits_gather<DIM, K, SH><<<blocks_g, 32 * GATHER_WARPS, smem_g, s>>>(D);
-        note_launches(1);
-        return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+        constexpr int OCC2 = GatherOccupancy<DIM, SH>::value;
+        constexpr int OCC3 = OCC2 > 1 ? OCC2 - 1 : 1;
+        return D.visit_kernel == 2 ? launch_gather<DIM, K, SH, OCC2>(D, s, sms)
+                                   : launch_gather<DIM, K, SH, OCC3>(D, s, sms);
     }
     if (D.visit_kernel == 1)
     {
@@ -987,6 +1011,7 @@ int
 launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s)
 {
     if (D.n_tiles == 0) return IBX_OK;
+    if (cudaMemsetAsync(D.work, 0, 2 * sizeof(int), s) != cudaSuccess) return IBX_E_CUDA;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

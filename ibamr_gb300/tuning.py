@@ -7,7 +7,8 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   tile+halo region rather than through per-tile visits (the split between
   the two spread kernels);
 * ``visit_kernel``: the form of the per-visit spread kernel (points
-  flattened over lanes, lane per visit, or the tile gathered in registers);
+  flattened over lanes, lane per visit, the tile gathered in registers, or
+  gathered with a larger register budget and fewer resident CTAs);
 * ``item_units``, ``dense_blocks_per_sm`` and ``unit_cap``: home units per
   CTA work item, CTAs per SM of the dense-tile kernel, and most markers per
   home unit (a unit is spread by one thread per component);
@@ -39,7 +40,7 @@ DEFAULT_CANDIDATES = {
     "dense_min": (8, 16, 32, 64, 128, 256),
     "item_units": (32, 64, 128, 256),
     "dense_blocks_per_sm": (1, 2, 4),
-    "visit_kernel": (0, 1, 2),
+    "visit_kernel": (0, 1, 2, 3),
     "interp_kernel": (0, 1, 2, 3, 4),
     "step_mode": (1, 0),
     "unit_cap": (32, 16, 8),

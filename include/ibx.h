@@ -229,9 +229,11 @@ int ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_prob
                      int precision, int tile_shape, ibx_plan** plan);
 int ibx_plan_tile_shape(const ibx_plan* plan, int* edges);
 int ibx_plan_bin(ibx_plan* plan, void* stream);
-/* One whole step: ibx_plan_bin, then ibx_plan_spread on `stream` and
- * ibx_plan_interpolate on a stream owned by the plan, running concurrently
- * (they read the same bins and write different arrays), joined back into
+/* One whole step: ibx_plan_bin on `stream`, then ibx_plan_spread and
+ * ibx_plan_interpolate on two streams owned by the plan, running
+ * concurrently (they read the same bins and write different arrays; the
+ * spread's stream has the device's greatest priority, the interpolation's
+ * the least, so the longer phase gets the SMs first), both joined back into
  * `stream` before the call's work ends.  Graph-capturable like the others. */
 int ibx_plan_step(ibx_plan* plan, void* stream);
 int ibx_plan_spread(ibx_plan* plan, void* stream);
@@ -271,7 +273,9 @@ int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, i
  * lanes, 1 = one lane per (visit, component) with all components of the
  * tile accumulated at once, 2 = the tile gathered: each lane owns values of
  * the tile in registers and adds every visit's separable weights, no
- * atomics (default).  Same results up to FP32 rounding. */
+ * atomics (default), 3 = form 2 compiled for one resident CTA per SM fewer
+ * (a larger register budget: no values spilled to local memory).  Same
+ * results up to FP32 rounding. */
 int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_visit_kernel(const ibx_plan* plan);
 /* Form of the interpolation (no reference counterpart; chosen by the

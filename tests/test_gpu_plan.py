@@ -265,7 +265,8 @@ def test_autotune_applies_a_measured_setting(ibx, oracle):
     plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED)
     res = tuning.autotune(plan, reps=1, candidates={"dense_min": (0, 32, 1 << 30), "item_units": (32, 256),
                                                     "dense_blocks_per_sm": (1, 2), "unit_cap": (32,)})
-    assert len(res["table"]) == 3 * 3 + 4 and res["visit_kernel"] in (0, 1, 2)
+    forms = tuning.DEFAULT_CANDIDATES["visit_kernel"]
+    assert len(res["table"]) == 3 * len(forms) + 4 and res["visit_kernel"] in forms
     assert plan.tuning() == res["best"] and plan.visit_kernel == res["visit_kernel"]
     cfg, ms = min(res["table"], key=lambda r: r[1])
     assert res["best"] == cfg[:3] and res["ms"] == ms
@@ -396,15 +397,15 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_for
     plan.close()
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 @pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 2)])
 def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_shape, form):
-    """The lane-per-(visit, component) form (1) and the tile-gather form (2)
-    of the per-visit kernel, every marker spread through its visits, against
-    the oracle."""
+    """The lane-per-(visit, component) form (1), the tile-gather form (2) and
+    the tile gather with a larger register budget (3) of the per-visit
+    kernel, every marker spread through its visits, against the oracle."""
     rng = np.random.default_rng(71 + dim + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     N = [29, 22, 18][:dim] if dim == 3 else [45, 38]
     n = 2500
@@ -551,3 +552,28 @@ def test_counting_sort_scans_small_and_large_tile_counts(ibx, N):
         assert abs(total - n) <= 1e-4 * n
     assert plan.status() == ibx.OK
     plan.close()
+
+
+@pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "BSPLINE_4", "IB_3"])
+@pytest.mark.parametrize("dim,N,n", [(3, [64, 64, 48], 5000), (3, [40, 48, 56], 3000), (2, [200, 180], 4000)])
+@pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
+def test_visit_gather_one_pass(ibx, oracle, kernel, dim, N, n, centering, depth):
+    """Sparse uniform markers (a few dozen visits per tile: one or two
+    batches) plus a cluster (tiles with hundreds of visits: many batches
+    folded into double-FP32 pairs), every tile spread through visits: the
+    gather forms 2 and 3 within the bar of the oracle."""
+    rng = np.random.default_rng(808 + N[0] + 17 * KERNEL_NAMES.index(kernel) + centering)
+    X = np.concatenate([rng.uniform(0.0, 1.0, size=(n, dim)), 0.3 + 0.01 * rng.standard_normal((n // 10, dim))])
+    X = np.mod(X, 1.0).reshape(-1)
+    m = X.size // dim
+    ncomp = dim if centering == 1 else depth
+    F = rng.standard_normal(m * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, _ = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
+    for form in (2, 3):
+        f, U, ps, pi = run_plan(ibx, dim, N, kernel, X, F, u, centering, depth, dense_min=1 << 30,
+                                visit_kernel=form)
+        assert ps.status() == ibx.OK
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL, form
+        ps.close()
+        pi.close()
