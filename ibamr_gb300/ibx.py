@@ -63,6 +63,10 @@ def lib():
         L.ibx_spring_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.ibx_cache_local_indices.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.c_void_p]
         L.ibx_redistribute.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         for name in ("ibx_accumulate_ghosts", "ibx_fill_ghosts"):
@@ -226,6 +230,44 @@ def redistribute(dim, boxes, X, stream=None):
     if rc:
         raise IbxError(rc, "ibx_redistribute")
     return owner, order, offsets
+
+
+class PatchGeometry(ctypes.Structure):
+    """ibx_patch_geometry: cell box, geometry and periodic boundary flags."""
+
+    _fields_ = [("dim", ctypes.c_int), ("ilower", ctypes.c_int * 3), ("iupper", ctypes.c_int * 3),
+                ("x_lower", ctypes.c_double * 3), ("x_upper", ctypes.c_double * 3), ("dx", ctypes.c_double * 3),
+                ("touches_periodic_lower", ctypes.c_int * 3), ("touches_periodic_upper", ctypes.c_int * 3)]
+
+
+def cache_local_indices(dim, ilower, iupper, x_lower, x_upper, dx, touches_periodic_lower, touches_periodic_upper,
+                        periodic_shift, ghost_width, want_ghost_box, X, capacity=None, stream=None):
+    """LIndexSetData::cacheLocalIndices on the device (ibx_cache_local_indices):
+    returns (local_indices int32, periodic_shifts float64 [dim per entry],
+    cells int32 [dim per entry]) device tensors.  X: device float64 tensor."""
+    import torch
+
+    G = PatchGeometry()
+    G.dim = dim
+    for d in range(dim):
+        G.ilower[d], G.iupper[d] = int(ilower[d]), int(iupper[d])
+        G.x_lower[d], G.x_upper[d], G.dx[d] = float(x_lower[d]), float(x_upper[d]), float(dx[d])
+        G.touches_periodic_lower[d] = int(touches_periodic_lower[d])
+        G.touches_periodic_upper[d] = int(touches_periodic_upper[d])
+    ps = (ctypes.c_int * 3)(*([int(v) for v in periodic_shift] + [0] * (3 - len(periodic_shift))))
+    gw = (ctypes.c_int * 3)(*([int(v) for v in ghost_width] + [0] * (3 - len(ghost_width))))
+    n = X.numel() // dim
+    cap = (3 ** dim) * max(n, 1) if capacity is None else int(capacity)
+    idx = torch.empty(max(cap, 1), dtype=torch.int32, device=X.device)
+    sh = torch.empty(max(cap, 1) * dim, dtype=torch.float64, device=X.device)
+    cells = torch.empty(max(cap, 1) * dim, dtype=torch.int32, device=X.device)
+    cnt = ctypes.c_int(0)
+    rc = lib().ibx_cache_local_indices(ctypes.byref(G), ps, gw, int(want_ghost_box), _ptr(X), int(n), int(cap),
+                                       _ptr(idx), _ptr(sh), _ptr(cells), ctypes.byref(cnt), _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_cache_local_indices")
+    m = cnt.value
+    return idx[:m], sh[: m * dim], cells[: m * dim]
 
 
 def spring_forces(dim, X, master, slave, stiffness, rest_length, F, accumulate=False, status=None, stream=None):

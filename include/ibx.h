@@ -170,6 +170,39 @@ typedef struct ibx_patch_box
 int ibx_redistribute(int dim, const ibx_patch_box* patches, int n_patches, const double* X, int n_markers, int* owner,
                      int* order, int* patch_offsets, void* stream);
 
+/* ---- cached index sets of a patch --------------------------------------- */
+/* One patch: cell box, CartesianPatchGeometry (getXLower/getXUpper/getDx)
+ * and getTouchesPeriodicBoundary(axis, 0/1). */
+typedef struct ibx_patch_geometry
+{
+    int dim;
+    int ilower[3], iupper[3];
+    double x_lower[3], x_upper[3], dx[3];
+    int touches_periodic_lower[3], touches_periodic_upper[3];
+} ibx_patch_geometry;
+
+/* LIndexSetData::cacheLocalIndices (ibtk/src/lagrangian/LIndexSetData.cpp:
+ * 50-140) on the device, for markers whose cells are given by their
+ * positions: marker s sits in cell c = getCellIndex(X_s) on the patch
+ * geometry (IndexUtilities-inl.h:52-75) and its periodic images in cells
+ * c + k * periodic_shift (k in {-1,0,1}^dim, k_d != 0 only where
+ * periodic_shift_d != 0).  Every image whose cell lies in the patch box grown
+ * by ghost_width (want_ghost_box != 0; the getLocalPETScIndices /
+ * getPeriodicShifts lists) or in the patch box (want_ghost_box == 0; the
+ * getInteriorLocalPETScIndices / getInteriorPeriodicShifts lists) and whose
+ * offset by the reference's rule (LIndexSetData.cpp:83-100: -periodic_shift
+ * below ilower at a lower periodic boundary, +periodic_shift above iupper at
+ * an upper one, else 0) equals k * periodic_shift is listed: local_indices[e]
+ * = s, periodic_shifts[dim*e + d] = offset_d * dx_d and, when cells is not
+ * NULL, cells[dim*e + d] = the image's cell.  Entries in marker order,
+ * images of a marker with k_0 fastest.  X, local_indices, periodic_shifts and
+ * cells are device arrays; *count (host) receives the number of entries.
+ * More entries than capacity: IBX_E_TOO_LARGE, the first capacity written.
+ * Uses stream-ordered scratch and synchronises the stream. */
+int ibx_cache_local_indices(const ibx_patch_geometry* patch, const int* periodic_shift, const int* ghost_width,
+                            int want_ghost_box, const double* X, int n_markers, int capacity, int* local_indices,
+                            double* periodic_shifts, int* cells, int* count, void* stream);
+
 /* ---- Lagrangian forces before spreading -------------------------------- */
 /* IBStandardForceGen::computeLagrangianSpringForce
  * (src/IB/IBStandardForceGen.cpp:825-900) with the default linear spring

@@ -63,3 +63,50 @@ def test_ghost_accumulation_01_3d_spread(programs, centering):
             assert abs(v - e[3]) <= 1e-13 * max(1.0, abs(e[3])), (comp_s, e, v)
             n += 1
     assert n == len(got) and n > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("centering,depth", [("side", 1), ("cell", 2)])
+@pytest.mark.parametrize("kernel", ["IB_4", "IB_6", "PIECEWISE_CUBIC", "BSPLINE_4"])
+def test_ldata_index_set_forms(programs, oracle, tmp_path, dim, centering, depth, kernel):
+    """The reference's LData / LIndexSetData signatures (SAMRAI::tbox::Pointer
+    handles, LIndexSetData::cacheLocalIndices on the device) against the
+    oracle's reference flow on a periodic patch (LDataManager::spread over
+    the ghost box, interp over the patch box) within 1e-12, and an
+    interpolation over a sub-box (buildLocalIndices' general path) equal to
+    the oracle's over the markers whose cell lies in it."""
+    import numpy as np
+
+    N = 32 if dim == 2 else 16
+    rng = np.random.default_rng(77 + dim + 3 * KERNELS.index(kernel) + (centering == "cell"))
+    n = 900
+    X = np.concatenate([rng.uniform(0.0, 1.0, size=(n // 2, dim)),
+                        np.mod(rng.uniform(-0.06, 0.06, size=(n - n // 2, dim)), 1.0)]).reshape(-1)
+    Q_depth = dim if centering == "side" else depth
+    ncomp = Q_depth
+    F = rng.standard_normal(n * Q_depth)
+    u = rng.standard_normal([ncomp] + [N] * dim)
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(inp, "wb") as fh:
+        fh.write(np.array([n, depth], dtype=np.int32).tobytes())
+        fh.write(X.tobytes())
+        fh.write(F.tobytes())
+        fh.write(u.reshape(-1).tobytes())
+    txt = run(programs[dim], "ldata", centering, kernel, str(N), str(inp), str(out))
+    assert txt.startswith("OK")
+    res = np.fromfile(out, dtype=np.float64)
+    f = res[: ncomp * N ** dim].reshape([ncomp] + [N] * dim)
+    U = res[ncomp * N ** dim: ncomp * N ** dim + n * Q_depth]
+    U_sub = res[ncomp * N ** dim + n * Q_depth:]
+    cen = 1 if centering == "side" else 0
+    f_ref, U_ref = oracle.periodic_problem(dim, [N] * dim, kernel, X, F=F, u=u, centering=cen, depth=depth)
+    assert np.max(np.abs(f - f_ref)) <= 1e-12 * np.max(np.abs(f_ref))
+    assert np.max(np.abs(U - U_ref)) <= 1e-12 * np.max(np.abs(U_ref))
+    # sub-box: the interior markers whose cell lies in [2, N - 3]^dim
+    cells = np.floor(X.reshape(n, dim) * N).astype(int)
+    inside = np.all((cells >= 2) & (cells <= N - 3), axis=1)
+    Us = U_sub.reshape(n, Q_depth)
+    Ur = U_ref.reshape(n, Q_depth)
+    assert np.all(Us[~inside] == 7.0)
+    assert np.max(np.abs(Us[inside] - Ur[inside])) <= 1e-12 * np.max(np.abs(Ur))
