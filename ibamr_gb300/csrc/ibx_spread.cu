@@ -753,10 +753,60 @@ struct GatherOccupancy
     static constexpr int value = GatherLayout<DIM, SH>::CPL > 16 ? 1 : 4;
 };
 
-// OCC: CTAs per SM the register budget is cut for (form 2: GatherOccupancy,
-// 64 registers for 3D tiles of 8^3, a few values spilled; form 3: one CTA per
-// SM fewer, no spills).
-template <int DIM, int K, int SH, int OCC>
+// The W weights of a stencil with base b, restricted to the E cells of a tile
+// starting at org (zero elsewhere), into dst.  PREP 0: dst was zeroed, the
+// in-tile weights are stored one by one (added when a grid narrower than the
+// stencil wraps two points onto one cell); PREP 1: the E values are formed in
+// registers and written with 16-byte stores.
+template <int W, int E, int PREP>
+__device__ __forceinline__ void
+put_weights(float* dst, const float* w, int b, int N, int org)
+{
+    if (PREP == 0)
+    {
+        const bool distinct = N >= W; // the stencil's points on distinct cells
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+        {
+            const int l = wrap_from_base(b + i, N) - org;
+            if (l >= 0 && l < E) dst[l] = distinct ? w[i] : dst[l] + w[i];
+        }
+    }
+    else
+    {
+        float vec[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) vec[j] = 0.f;
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+        {
+            const int l = wrap_from_base(b + i, N) - org;
+#pragma unroll
+            for (int j = 0; j < E; ++j) vec[j] = l == j ? vec[j] + w[i] : vec[j];
+        }
+        if (E % 4 == 0)
+        {
+#pragma unroll
+            for (int j = 0; j < E; j += 4)
+                *reinterpret_cast<float4*>(dst + j) = make_float4(vec[j], vec[j + 1], vec[j + 2], vec[j + 3]);
+        }
+        else
+        {
+#pragma unroll
+            for (int j = 0; j < E; ++j) dst[j] = vec[j];
+        }
+    }
+}
+
+// OCC: CTAs per SM the register budget is cut for (GatherOccupancy: 64
+// registers for 3D tiles of 8^3).  PREP: how a lane writes its visit's
+// tile-restricted weight vectors into its slot -- 0: the slot is zeroed with
+// 16-byte stores and the in-tile weights stored one by one (added when a
+// grid narrower than the stencil wraps two points onto one cell); 1: each
+// vector is assembled in registers (a compare and select per tile position
+// and stencil point) and written with 16-byte stores, no zeroing (form 3:
+// fewer shared-memory wavefronts, more arithmetic).
+template <int DIM, int K, int SH, int OCC, int PREP>
 __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(const DevPlan D)
 {
     constexpr int W = KT<K>::W;
@@ -800,8 +850,13 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
             {
                 const int nb = min(32, vend - b0);
                 // -- this lane's visit: its weight vectors restricted to the tile
+                //    (only the slots of the batch's visits are read)
+                if (PREP == 0)
+                {
 #pragma unroll
-                for (int i = 0; i < SS / 4; ++i) reinterpret_cast<float4*>(mine)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int i = 0; i < SS / 4; ++i)
+                        reinterpret_cast<float4*>(mine)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
                 if (lane < nb)
                 {
                     const int g = D.visit_list[b0 + lane];
@@ -815,13 +870,18 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
                         float w[W];
                         weights_f32<K>(stag ? R.rs[d] : R.rc[d], w);
                         const int off = d == 0 ? 0 : d == 1 ? T::E0 : T::E0 + T::E1;
-#pragma unroll
-                        for (int i = 0; i < W; ++i)
+                        // Q/vol rides on the last dimension's weights
+                        if (d == DIM - 1)
                         {
-                            const int l = wrap_from_base(b + i, P.N[d]) - org[d];
-                            // Q/vol rides on the last dimension's weights
-                            if (l >= 0 && l < T::edge(d)) mine[off + l] += d == DIM - 1 ? w[i] * V : w[i];
+#pragma unroll
+                            for (int i = 0; i < W; ++i) w[i] *= V;
                         }
+                        if (d == 0)
+                            put_weights<W, T::E0, PREP>(mine + off, w, b, P.N[d], org[d]);
+                        else if (d == 1)
+                            put_weights<W, T::E1, PREP>(mine + off, w, b, P.N[d], org[d]);
+                        else
+                            put_weights<W, T::E2, PREP>(mine + off, w, b, P.N[d], org[d]);
                     }
                 }
                 __syncwarp();
@@ -927,23 +987,23 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
 
 namespace
 {
-template <int DIM, int K, int SH, int OCC>
+template <int DIM, int K, int SH, int OCC, int PREP>
 int
 launch_gather(const DevPlan& D, cudaStream_t s, int sms)
 {
     using GL = GatherLayout<DIM, SH>;
     const size_t smem_g = sizeof(float) * 32 * GL::SS * GATHER_WARPS;
     if (smem_g > 48 * 1024 &&
-        cudaFuncSetAttribute(spread_visits_gather<DIM, K, SH, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(spread_visits_gather<DIM, K, SH, OCC, PREP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_g) != cudaSuccess)
         return IBX_E_CUDA;
     int per_sm_g = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_g, spread_visits_gather<DIM, K, SH, OCC>, 32 * GATHER_WARPS,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_g, spread_visits_gather<DIM, K, SH, OCC, PREP>, 32 * GATHER_WARPS,
                                                   smem_g);
     if (per_sm_g < 1) per_sm_g = 1;
     const unsigned need_g = (unsigned)((D.n_tiles + GATHER_WARPS - 1) / GATHER_WARPS);
     const unsigned blocks_g = need_g < (unsigned)(per_sm_g * sms) ? need_g : (unsigned)(per_sm_g * sms);
-    spread_visits_gather<DIM, K, SH, OCC><<<blocks_g, 32 * GATHER_WARPS, smem_g, s>>>(D);
+    spread_visits_gather<DIM, K, SH, OCC, PREP><<<blocks_g, 32 * GATHER_WARPS, smem_g, s>>>(D);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
@@ -968,10 +1028,9 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
     }
     if (D.visit_kernel == 2 || D.visit_kernel == 3)
     {
-        constexpr int OCC2 = GatherOccupancy<DIM, SH>::value;
-        constexpr int OCC3 = OCC2 > 1 ? OCC2 - 1 : 1;
-        return D.visit_kernel == 2 ? launch_gather<DIM, K, SH, OCC2>(D, s, sms)
-                                   : launch_gather<DIM, K, SH, OCC3>(D, s, sms);
+        constexpr int OCC = GatherOccupancy<DIM, SH>::value;
+        return D.visit_kernel == 2 ? launch_gather<DIM, K, SH, OCC, 0>(D, s, sms)
+                                   : launch_gather<DIM, K, SH, OCC, 1>(D, s, sms);
     }
     if (D.visit_kernel == 1)
     {

@@ -8,7 +8,7 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   the two spread kernels);
 * ``visit_kernel``: the form of the per-visit spread kernel (points
   flattened over lanes, lane per visit, the tile gathered in registers, or
-  gathered with a larger register budget and fewer resident CTAs);
+  gathered with the visits' weight vectors assembled in registers);
 * ``item_units``, ``dense_blocks_per_sm`` and ``unit_cap``: home units per
   CTA work item, CTAs per SM of the dense-tile kernel, and most markers per
   home unit (a unit is spread by one thread per component);

@@ -306,9 +306,10 @@ int ibx_plan_get_tuning(const ibx_plan* plan, int* item_units, int* dense_min, i
  * lanes, 1 = one lane per (visit, component) with all components of the
  * tile accumulated at once, 2 = the tile gathered: each lane owns values of
  * the tile in registers and adds every visit's separable weights, no
- * atomics (default), 3 = form 2 compiled for one resident CTA per SM fewer
- * (a larger register budget: no values spilled to local memory).  Same
- * results up to FP32 rounding. */
+ * atomics (default), 3 = form 2 with each visit's tile-restricted weight
+ * vectors assembled in registers and written with 16-byte stores (fewer
+ * shared-memory accesses, more arithmetic).  Same results up to FP32
+ * rounding. */
 int ibx_plan_set_visit_kernel(ibx_plan* plan, int form);
 int ibx_plan_get_visit_kernel(const ibx_plan* plan);
 /* Form of the interpolation (no reference counterpart; chosen by the

@@ -404,8 +404,9 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_for
 @pytest.mark.parametrize("centering,depth", [(1, 1), (0, 2)])
 def test_visit_kernel_forms(ibx, oracle, kernel, dim, centering, depth, tile_shape, form):
     """The lane-per-(visit, component) form (1), the tile-gather form (2) and
-    the tile gather with a larger register budget (3) of the per-visit
-    kernel, every marker spread through its visits, against the oracle."""
+    the tile gather with register-assembled weight vectors (3) of the
+    per-visit kernel, every marker spread through its visits, against the
+    oracle."""
     rng = np.random.default_rng(71 + dim + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
     N = [29, 22, 18][:dim] if dim == 3 else [45, 38]
     n = 2500
