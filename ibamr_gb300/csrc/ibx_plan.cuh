@@ -283,12 +283,12 @@ wrap_from_base(int x, int N)
 }
 
 // ---- FP32 weights (mixed form) --------------------------------------------
-// sqrt(a) for a > 0 through the hardware reciprocal square root (a few ulp;
-// the mixed form's weights are FP32 values anyway), 0 for a <= 0.
+// sqrt(a) rounded to nearest for a > 0 (the IEEE square root of CUDA's
+// __fsqrt_rn), 0 for a <= 0.
 __device__ __forceinline__ float
 sqrt_f32(float a)
 {
-    return a > 0.f ? a * rsqrtf(a) : 0.f;
+    return a > 0.f ? __fsqrt_rn(a) : 0.f;
 }
 
 __device__ __forceinline__ float
