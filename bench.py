@@ -66,7 +66,7 @@ def parse_args():
     ap.add_argument("--tune", action="store_true", help="run the autotuner on the helices workload")
     ap.add_argument("--no-tune", action="store_true", help="library defaults on the helices workload")
     ap.add_argument("--setting", default=None,
-                    help="fixed plan setting k=v,... as printed under tuning.setting (helices workload)")
+                    help="fixed plan setting k=v,... as printed under tuning.setting (helices or batched workload)")
     ap.add_argument("--kernel", default="IB_4", choices=sorted(KERNEL_WIDTHS),
                     help="delta kernel of the helices workload (the metric is quoted on IB_4)")
     ap.add_argument("--workload", default="all", choices=["all", "helices", "batched", "serving"],
@@ -755,7 +755,7 @@ def run_ours(args):
     else:
         mode = "pinned"
     if args.workload == "batched":
-        line = batched_case(args, dev, world, with_cpu, args.steps, args.warmup)
+        line = batched_case(args, dev, world, with_cpu, args.steps, args.warmup, setting=args.setting)
     elif args.workload == "serving":
         line = serving_case(args, dev, world, with_cpu, args.steps)
     else:
