@@ -67,6 +67,11 @@ def lib():
                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                               ctypes.c_void_p]
+        L.ibx_fe_quadrature_points.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]
+        L.ibx_fe_assemble_rhs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
         L.ibx_redistribute.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         for name in ("ibx_accumulate_ghosts", "ibx_fill_ghosts"):
@@ -268,6 +273,69 @@ def cache_local_indices(dim, ilower, iupper, x_lower, x_upper, dx, touches_perio
         raise IbxError(rc, "ibx_cache_local_indices")
     m = cnt.value
     return idx[:m], sh[: m * dim], cells[: m * dim]
+
+
+class FeMesh(ctypes.Structure):
+    """ibx_fe_mesh: first-order simplex mesh (device arrays)."""
+
+    _fields_ = [("dim", ctypes.c_int), ("n_nodes", ctypes.c_int), ("n_elems", ctypes.c_int),
+                ("elem_nodes", ctypes.c_void_p), ("X", ctypes.c_void_p)]
+
+
+class QuadRule(ctypes.Structure):
+    """ibx_quad_rule: reference points and weights (host arrays)."""
+
+    _fields_ = [("n_points", ctypes.c_int), ("points", ctypes.c_void_p), ("weights", ctypes.c_void_p)]
+
+
+def _fe_args(dim, elem_nodes, X, points, weights):
+    import numpy as np
+
+    M = FeMesh()
+    M.dim = dim
+    M.n_nodes = X.numel() // dim
+    M.n_elems = elem_nodes.numel() // (dim + 1)
+    M.elem_nodes = _ptr(elem_nodes).value
+    M.X = _ptr(X).value
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+    w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+    R = QuadRule()
+    R.n_points = w.size
+    R.points = pts.ctypes.data
+    R.weights = w.ctypes.data
+    return M, R, (pts, w)
+
+
+def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0, stream=None):
+    """FEDataManager::spread's quadrature points (ibx_fe_quadrature_points):
+    returns (X_qp, F_JxW_qp or None, JxW) float64 device tensors."""
+    import torch
+
+    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights)
+    nq = M.n_elems * R.n_points
+    X_qp = torch.empty(max(nq, 1) * dim, dtype=torch.float64, device=X.device)
+    JxW = torch.empty(max(nq, 1), dtype=torch.float64, device=X.device)
+    F_qp = torch.empty(max(nq, 1) * max(n_vars, 1), dtype=torch.float64, device=X.device) if F is not None else None
+    status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    rc = lib().ibx_fe_quadrature_points(ctypes.byref(M), ctypes.byref(R), _ptr(F), int(n_vars), _ptr(X_qp),
+                                        _ptr(F_qp), _ptr(JxW), _ptr(status), _stream_handle(stream))
+    del keep
+    if rc:
+        raise IbxError(rc, "ibx_fe_quadrature_points")
+    if int(status.item()):
+        raise IbxError(E_ARG, "ibx_fe_quadrature_points: negative node index")
+    return X_qp[: nq * dim], None if F_qp is None else F_qp[: nq * n_vars], JxW[:nq]
+
+
+def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars, rhs, stream=None):
+    """FEDataManager::interp's right-hand side (ibx_fe_assemble_rhs): adds into
+    rhs (float64 device tensor, n_vars per node)."""
+    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights)
+    rc = lib().ibx_fe_assemble_rhs(ctypes.byref(M), ctypes.byref(R), _ptr(U_qp), int(n_vars), _ptr(rhs),
+                                   _stream_handle(stream))
+    del keep
+    if rc:
+        raise IbxError(rc, "ibx_fe_assemble_rhs")
 
 
 def spring_forces(dim, X, master, slave, stiffness, rest_length, F, accumulate=False, status=None, stream=None):

@@ -203,6 +203,56 @@ int ibx_cache_local_indices(const ibx_patch_geometry* patch, const int* periodic
                             int want_ghost_box, const double* X, int n_markers, int capacity, int* local_indices,
                             double* periodic_shifts, int* cells, int* count, void* stream);
 
+/* ---- finite-element quadrature points (FEDataManager) ------------------- */
+/* A mesh of first-order Lagrange simplices (TRI3 in 2D, TET4 in 3D): node k
+ * of element e is elem_nodes[(dim+1)*e + k] (libMesh's vertex order: the
+ * reference element's vertices 0, e_1, ..., e_dim); X holds dim coordinates
+ * per node.  Both are device arrays. */
+typedef struct ibx_fe_mesh
+{
+    int dim;
+    int n_nodes;
+    int n_elems;
+    const int* elem_nodes;
+    const double* X;
+} ibx_fe_mesh;
+
+/* A quadrature rule on the reference simplex (host arrays): n_points points
+ * (dim reference coordinates each) and their weights (summing to the
+ * reference element's measure, 1/2 in 2D and 1/6 in 3D, as libMesh's
+ * rules do); at most 64 points. */
+typedef struct ibx_quad_rule
+{
+    int n_points;
+    const double* points;
+    const double* weights;
+} ibx_quad_rule;
+
+/* The quadrature-point side of FEDataManager::spread
+ * (ibtk/src/lagrangian/FEDataManager.cpp:1088-1219, sum_weighted_elem_solution
+ * :824-858): for point q of element e (entry e*n_points + q),
+ * X_qp = sum_k X_k phi_k(q) and, when F_nodes is given (n_vars values per
+ * node), F_JxW_qp = (sum_k F_k phi_k(q)) * JxW(q), with the barycentric basis
+ * phi and JxW(q) = |det J| * weight(q); JxW receives JxW(q) when not NULL.
+ * Sums run from zero over the basis in order, every operation rounded as
+ * written.  The outputs feed ibx_spread (positions X_qp, values F_JxW_qp) as
+ * LEInteractor::spread's raw-array form does in the reference.  An element
+ * with a negative node index is skipped and sets bit 0 of the device word
+ * *status.  Device pointers; stream-ordered. */
+int ibx_fe_quadrature_points(const ibx_fe_mesh* mesh, const ibx_quad_rule* rule, const double* F_nodes, int n_vars,
+                             double* X_qp, double* F_JxW_qp, double* JxW, int* status, void* stream);
+
+/* The assembly side of FEDataManager::interp (FEDataManager.cpp:1873-2005,
+ * integrate_elem_rhs :1569-1604): with U_qp the values interpolated at the
+ * quadrature points (n_vars per point, as ibx_interpolate writes them at
+ * X_qp), rhs[n_vars*node + i] += sum_q U_qp[q][i] * (phi_k(q) * JxW(q)) for
+ * every element and every node k of it -- the right-hand side of the L2
+ * projection (the projection's solve is the caller's).  Element sums in point
+ * order; elements are added with FP64 atomics (their order may differ from
+ * the reference's vector assembly).  Device pointers; stream-ordered. */
+int ibx_fe_assemble_rhs(const ibx_fe_mesh* mesh, const ibx_quad_rule* rule, const double* U_qp, int n_vars,
+                        double* rhs, void* stream);
+
 /* ---- Lagrangian forces before spreading -------------------------------- */
 /* IBStandardForceGen::computeLagrangianSpringForce
  * (src/IB/IBStandardForceGen.cpp:825-900) with the default linear spring

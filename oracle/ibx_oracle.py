@@ -333,3 +333,80 @@ class CpuPlan:
         if getattr(self, "h", None):
             lib().ibxo_cpu_plan_destroy(self.h)
             self.h = None
+
+
+# ---------------------------------------------------------------------------
+# Finite-element quadrature points (FEDataManager, first-order simplices).
+# ---------------------------------------------------------------------------
+
+def _fe_phi(dim, points):
+    """Barycentric basis at the reference points: phi_0 = 1 - (xi_0 + ... ),
+    phi_d = xi_d (first-order Lagrange TRI3 / TET4)."""
+    P = np.asarray(points, dtype=np.float64).reshape(-1, dim)
+    s = np.zeros(P.shape[0])
+    for d in range(dim):
+        s = s + P[:, d]
+    return np.concatenate([(1.0 - s)[:, None], P], axis=1)  # [n_qp, dim + 1]
+
+
+def _fe_abs_det(dim, elem_nodes, X):
+    E = np.asarray(elem_nodes).reshape(-1, dim + 1)
+    Xn = np.asarray(X, dtype=np.float64).reshape(-1, dim)
+    J = np.stack([Xn[E[:, c + 1]] - Xn[E[:, 0]] for c in range(dim)], axis=2)  # J[e, r, c]
+    if dim == 2:
+        det = J[:, 0, 0] * J[:, 1, 1] - J[:, 0, 1] * J[:, 1, 0]
+    else:
+        m0 = J[:, 1, 1] * J[:, 2, 2] - J[:, 1, 2] * J[:, 2, 1]
+        m1 = J[:, 1, 0] * J[:, 2, 2] - J[:, 1, 2] * J[:, 2, 0]
+        m2 = J[:, 1, 0] * J[:, 2, 1] - J[:, 1, 1] * J[:, 2, 0]
+        det = (J[:, 0, 0] * m0 - J[:, 0, 1] * m1) + J[:, 0, 2] * m2
+    return np.abs(det)
+
+
+def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0):
+    """FEDataManager::spread's quadrature-point values
+    (ibtk/src/lagrangian/FEDataManager.cpp:1088-1219 with
+    sum_weighted_elem_solution :824-858): X_q = sum_k X_k phi_k(q) and
+    F_q = (sum_k F_k phi_k(q)) * JxW(q), the sums from zero over the basis in
+    order, JxW(q) = |det J| * w(q).  Returns (X_qp, F_qp or None, JxW),
+    entries e * n_qp + q."""
+    E = np.asarray(elem_nodes).reshape(-1, dim + 1)
+    Xn = np.asarray(X, dtype=np.float64).reshape(-1, dim)
+    phi = _fe_phi(dim, points)
+    w = np.asarray(weights, dtype=np.float64).reshape(-1)
+    nq = w.size
+    ne = E.shape[0]
+    X_qp = np.zeros((ne, nq, dim))
+    for k in range(dim + 1):
+        X_qp = X_qp + Xn[E[:, k]][:, None, :] * phi[None, :, k, None]
+    jxw = _fe_abs_det(dim, elem_nodes, X)[:, None] * w[None, :]
+    F_qp = None
+    if F is not None:
+        Fn = np.asarray(F, dtype=np.float64).reshape(-1, n_vars)
+        acc = np.zeros((ne, nq, n_vars))
+        for k in range(dim + 1):
+            acc = acc + Fn[E[:, k]][:, None, :] * phi[None, :, k, None]
+        F_qp = (acc * jxw[:, :, None]).reshape(-1)
+    return X_qp.reshape(-1), F_qp, jxw.reshape(-1)
+
+
+def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars):
+    """FEDataManager::interp's right-hand side (FEDataManager.cpp:1873-2005,
+    integrate_elem_rhs :1569-1604): rhs[node_k] += sum_q U_q * (phi_k(q) *
+    JxW(q)) per element, the element sums in point order, the elements added
+    in order.  Returns rhs [n_nodes * n_vars]."""
+    E = np.asarray(elem_nodes).reshape(-1, dim + 1)
+    n_nodes = np.asarray(X).size // dim
+    phi = _fe_phi(dim, points)
+    w = np.asarray(weights, dtype=np.float64).reshape(-1)
+    nq = w.size
+    det = _fe_abs_det(dim, elem_nodes, X)
+    U = np.asarray(U_qp, dtype=np.float64).reshape(E.shape[0], nq, n_vars)
+    rhs = np.zeros((n_nodes, n_vars))
+    for k in range(dim + 1):
+        acc = np.zeros((E.shape[0], n_vars))
+        for q in range(nq):
+            p_jxw = phi[q, k] * (det * w[q])
+            acc = acc + U[:, q, :] * p_jxw[:, None]
+        np.add.at(rhs, E[:, k], acc)
+    return rhs.reshape(-1)
