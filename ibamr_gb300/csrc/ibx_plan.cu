@@ -373,6 +373,7 @@ ibx_plan_step(ibx_plan* plan, void* stream)
         rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
         return rc ? rc : launch_interp(plan->dim, plan->kernel, plan->D, s);
     }
+    if (plan->step_mode == 2) return launch_fused(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
     // spread and interpolation read the same records and write different
     // arrays: they overlap on the device, the spread's blocks dispatched first
     if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
@@ -493,7 +494,7 @@ ibx_plan_get_unit_cap(const ibx_plan* plan)
 int
 ibx_plan_set_step_mode(ibx_plan* plan, int mode)
 {
-    if (!plan || mode < 0 || mode > 1) return IBX_E_ARG;
+    if (!plan || mode < 0 || mode > 2) return IBX_E_ARG;
     plan->step_mode = mode;
     return IBX_OK;
 }

@@ -390,6 +390,9 @@ int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 int exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s);
 int launch_items_fill(const DevPlan& D, cudaStream_t s);
 int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
+// Spread and interpolation of the binned markers in one persistent launch
+// (ibx_spread.cu: step_fused).
+int launch_fused(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
 int launch_interp(int dim, int kernel, const DevPlan& D, cudaStream_t s);
 
 } // namespace ibx

@@ -23,7 +23,7 @@
 // Product order per contribution: w0 * (w1 * (w2 * (Q/vol))), the
 // association of the reference's tensor-product kernels (F3D:1436-1468).
 
-#include "ibx_plan.cuh"
+#include "ibx_interp_body.cuh" // the interpolation bodies the fused step kernel runs
 #include "../../include/ibx.h"
 
 namespace ibx
@@ -136,8 +136,12 @@ struct HomeOccupancy
     static constexpr int value = DIM == 3 ? 3 : 4;
 };
 
+// One dense work item, by every thread of a CTA of UNIT_THREADS (it holds
+// CTA barriers and ends with one): sm is the CTA's region buffer
+// ([ncomp][hi, lo][PAD], components CSTR apart).
 template <int DIM, int K, int SH>
-__global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) spread_home_mixed(const DevPlan D)
+__device__ __forceinline__ void
+dense_item(const DevPlan& D, int item, float* sm)
 {
     constexpr int W = KT<K>::W;
     using RG = Region<DIM, W, SH>;
@@ -146,17 +150,7 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
     constexpr int PAD = RG::PAD;
     constexpr int CSTR = RG::CSTR;
     constexpr int NF = RG::NF;
-    extern __shared__ float sm[]; // [ncomp][hi, lo][PAD], components CSTR apart
-    __shared__ int s_item;
-    const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
-    // Work items are taken from a counter, so that CTAs that become resident
-    // late (beside other kernels, or in a second wave) do not leave a tail.
-    for (;;)
     {
-        if (threadIdx.x == 0) s_item = atomicAdd(&D.work[0], 1);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= n_items) break;
         const int t = D.item_tile[item];
         const int k = item - D.items[t];
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
@@ -382,6 +376,25 @@ __global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) sprea
         for (int c = 0; c < ncomp; ++c)
             region_flush<DIM, W, SH>(P, org, c, sm + c * CSTR, sm + c * CSTR + PAD, threadIdx.x, blockDim.x);
         __syncthreads();
+    }
+    (void)NF;
+}
+
+template <int DIM, int K, int SH>
+__global__ void __launch_bounds__(UNIT_THREADS, HomeOccupancy<DIM>::value) spread_home_mixed(const DevPlan D)
+{
+    extern __shared__ float sm[]; // [ncomp][hi, lo][PAD], components CSTR apart
+    __shared__ int s_item;
+    const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
+    // Work items are taken from a counter, so that CTAs that become resident
+    // late (beside other kernels, or in a second wave) do not leave a tail.
+    for (;;)
+    {
+        if (threadIdx.x == 0) s_item = atomicAdd(&D.work[0], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items) break;
+        dense_item<DIM, K, SH>(D, item, sm);
     }
 }
 
@@ -798,25 +811,24 @@ put_weights(float* dst, const float* w, int b, int N, int org)
     }
 }
 
-// OCC: CTAs per SM the register budget is cut for (GatherOccupancy: 64
-// registers for 3D tiles of 8^3).  PREP: how a lane writes its visit's
+// Tile t's visits gathered by one warp (every lane); slots: the warp's 32
+// visit slots of SS floats.  PREP: how a lane writes its visit's
 // tile-restricted weight vectors into its slot -- 0: the slot is zeroed with
 // 16-byte stores and the in-tile weights stored one by one (added when a
 // grid narrower than the stencil wraps two points onto one cell); 1: each
 // vector is assembled in registers (a compare and select per tile position
 // and stencil point) and written with 16-byte stores, no zeroing (form 3:
-// fewer shared-memory wavefronts, more arithmetic).
-template <int DIM, int K, int SH, int OCC, int PREP>
-__global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(const DevPlan D)
+// fewer shared-memory wavefronts, more arithmetic).  The grid values are read
+// through L2 only (each is read once).
+template <int DIM, int K, int SH, int PREP>
+__device__ __forceinline__ void
+gather_tile(const DevPlan& D, int t, float* slots, int lane)
 {
     constexpr int W = KT<K>::W;
     using T = TileT<DIM, SH>;
     using GL = GatherLayout<DIM, SH>;
     constexpr int CPL = GL::CPL, SX = GL::SX, NR = GL::NR, SS = GL::SS;
     constexpr int SP = SX / 2; // value pairs per lane row
-    extern __shared__ float sm[]; // [GATHER_WARPS][32][SS]
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* slots = sm + warp * 32 * SS;
     float* mine = slots + lane * SS;
     // This lane's values: NR consecutive rows y0 .. y0 + NR - 1 of plane z
     // (rows are y + E1 * z; NR and E1 are even or NR is 1), x in [xs, xs + SX).
@@ -826,16 +838,10 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
     const int y0 = r0 % T::E1;
     const int z0 = r0 / T::E1;
     static_assert(NR == 1 || (NR == 2 && T::E1 % 2 == 0), "a lane's rows share their plane");
-    // each warp takes its next tile from a counter (no tail from late CTAs)
-    for (;;)
     {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(&D.work[1], 1);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= D.n_tiles) break;
         const int vbeg = D.vcount[t];
         const int vend = (long long)D.vcount[t + 1] < D.n_visit_cap ? D.vcount[t + 1] : (int)D.n_visit_cap;
-        if (vend <= vbeg) continue;
+        if (vend <= vbeg) return;
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
         const PlanProb& P = D.probs[p];
         int org[3];
@@ -963,7 +969,7 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
                         continue;
                     if (vec)
                     {
-                        float4 v = *reinterpret_cast<float4*>(q + o + i);
+                        float4 v = __ldcg(reinterpret_cast<const float4*>(q + o + i));
                         v.x = merge3(v.x, h[0], l[0]);
                         v.y = merge3(v.y, h[1], l[1]);
                         v.z = merge3(v.z, h[2], l[2]);
@@ -975,12 +981,131 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(c
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
                             if (x0 + i + e < P.N[0] && (h[e] != 0.f || l[e] != 0.f))
-                                q[o + i + e] = merge3(q[o + i + e], h[e], l[e]);
+                                q[o + i + e] = merge3(__ldcg(q + o + i + e), h[e], l[e]);
                     }
                 }
             }
         }
     }
+}
+
+// OCC: CTAs per SM the register budget is cut for (GatherOccupancy: 64
+// registers for 3D tiles of 8^3).
+template <int DIM, int K, int SH, int OCC, int PREP>
+__global__ void __launch_bounds__(32 * GATHER_WARPS, OCC) spread_visits_gather(const DevPlan D)
+{
+    using GL = GatherLayout<DIM, SH>;
+    extern __shared__ float sm[]; // [GATHER_WARPS][32][SS]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* slots = sm + warp * 32 * GL::SS;
+    // each warp takes its next tile from a counter (no tail from late CTAs)
+    for (;;)
+    {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&D.work[1], 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= D.n_tiles) break;
+        gather_tile<DIM, K, SH, PREP>(D, t, slots, lane);
+    }
+}
+
+// ---- the post-binning step in one persistent launch ------------------------
+// Every CTA takes work from one device counter, in this order: the dense
+// spread's work items (dense_item), the per-unit interpolation of the same
+// items (units_item), the chunked interpolation of the sparse-homed markers
+// (chunk_body, no register cache; every marker where the per-unit form does
+// not apply), and groups of GATHER_WARPS tiles of the
+// per-visit gather spread (gather_tile, one warp per tile).  The gather adds
+// into tiles that the dense items' region atomics also reach, so a gather
+// group first waits until every dense item has finished -- a counter the
+// dense items raise after a device-wide fence.  Every dense item was claimed
+// before any gather group (counter order) by a CTA that is running, so the
+// wait ends; it is bounded all the same (about a second), reported through
+// bit 2 of the status word.  One launch for the spread and the interpolation
+// of every problem of the plan; the phases share the SMs as their work
+// arrives instead of partitioning them between two streams.
+constexpr int FUSED_THREADS = 256;
+constexpr int DONE_SPINS = 1 << 22;
+static_assert(FUSED_THREADS == UNIT_THREADS && FUSED_THREADS == INTERP_THREADS &&
+                  FUSED_THREADS == 32 * GATHER_WARPS,
+              "one CTA shape for every phase");
+
+template <int DIM, int K, int SH, int PREP>
+__global__ void __launch_bounds__(FUSED_THREADS, 3) step_fused(const DevPlan D)
+{
+    using GL = GatherLayout<DIM, SH>;
+    extern __shared__ float sm[]; // the dense region buffer, or the warps' visit slots
+    __shared__ int s_item;
+    __shared__ int s_order[256];
+    __shared__ int s_start[33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nD = min(D.items[D.n_tiles], D.n_item_cap);
+    const long long chunk_threads = (D.n_markers + CHUNK - 1) / CHUNK * D.max_ncomp;
+    const int nC = (int)((chunk_threads + FUSED_THREADS - 1) / FUSED_THREADS);
+    const int nG = (D.n_tiles + GATHER_WARPS - 1) / GATHER_WARPS;
+    // the per-unit interpolation holds a unit's stencil values in registers
+    // only up to 64 per lane; beyond that the chunks take every marker
+    constexpr bool UNITS = UnitSplit<DIM, KT<K>::W>::NC <= 64;
+    const int nU = UNITS ? nD : 0;
+    const int total = nD + nU + nC + nG;
+    for (;;)
+    {
+        __syncthreads(); // the previous piece of work is done with s_item, s_order and sm
+        if (threadIdx.x == 0) s_item = atomicAdd(&D.work[0], 1);
+        __syncthreads();
+        const int w = s_item;
+        if (w >= total) break;
+        if (w < nD)
+        {
+            dense_item<DIM, K, SH>(D, w, sm);
+            __threadfence(); // this thread's region atomics, visible device-wide
+            __syncthreads();
+            if (threadIdx.x == 0) atomicAdd(&D.work[1], 1);
+        }
+        else if (w < nD + nU)
+            units_item<DIM, K>(D, w - nD, s_order, s_start);
+        else if (w < nD + nU + nC)
+            chunk_body<DIM, K, false>(D, (long long)(w - nD - nU) * FUSED_THREADS + threadIdx.x,
+                                      UNITS ? SEL_SPARSE : SEL_ALL, 0);
+        else
+        {
+            if (threadIdx.x == 0)
+            {
+                for (int spins = 0; atomicAdd(&D.work[1], 0) < nD; ++spins)
+                {
+                    if (spins >= DONE_SPINS)
+                    {
+                        atomicOr(D.status, 4);
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+                __threadfence();
+            }
+            __syncthreads();
+            const int t = (w - nD - nU - nC) * GATHER_WARPS + warp;
+            if (t < D.n_tiles) gather_tile<DIM, K, SH, PREP>(D, t, sm + warp * 32 * GL::SS, lane);
+        }
+    }
+}
+
+template <int DIM, int K, int SH, int PREP>
+int
+launch_fused_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
+{
+    constexpr int W = KT<K>::W;
+    const size_t smem_d = sizeof(float) * Region<DIM, W, SH>::CSTR * max_ncomp;
+    const size_t smem_g = sizeof(float) * 32 * GatherLayout<DIM, SH>::SS * GATHER_WARPS;
+    const size_t smem = smem_d > smem_g ? smem_d : smem_g;
+    if (cudaFuncSetAttribute(step_fused<DIM, K, SH, PREP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return IBX_E_CUDA;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_fused<DIM, K, SH, PREP>, FUSED_THREADS, smem);
+    if (per_sm < 1) per_sm = 1;
+    step_fused<DIM, K, SH, PREP><<<(unsigned)(per_sm * sms), FUSED_THREADS, smem, s>>>(D);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 } // namespace
@@ -1065,6 +1190,26 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 } // namespace
+
+int
+launch_fused(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s)
+{
+    if (D.n_tiles == 0) return IBX_OK;
+    if (cudaMemsetAsync(D.work, 0, 2 * sizeof(int), s) != cudaSuccess) return IBX_E_CUDA;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // the gather phase in its plain form (visit forms 2 and 3 give the same sums)
+    const int sh = D.tile_shape;
+#define IBX_FUSED_CASE(DD, KK)                                                                                       \
+    if (dim == DD && kernel == KK)                                                                                   \
+        return sh == 0 ? launch_fused_k<DD, KK, 0, 0>(D, max_ncomp, s, sms) : launch_fused_k<DD, KK, 1, 0>(D, max_ncomp, s, sms);
+    IBX_FUSED_CASE(2, K_PL) IBX_FUSED_CASE(2, K_PCUBIC) IBX_FUSED_CASE(2, K_IB3) IBX_FUSED_CASE(2, K_IB4)
+    IBX_FUSED_CASE(2, K_IB6) IBX_FUSED_CASE(2, K_BSPL4) IBX_FUSED_CASE(3, K_PL) IBX_FUSED_CASE(3, K_PCUBIC)
+    IBX_FUSED_CASE(3, K_IB3) IBX_FUSED_CASE(3, K_IB4) IBX_FUSED_CASE(3, K_IB6) IBX_FUSED_CASE(3, K_BSPL4)
+#undef IBX_FUSED_CASE
+    return IBX_E_BAD_KERNEL;
+}
 
 int
 launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s)

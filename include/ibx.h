@@ -324,8 +324,9 @@ int ibx_plan_interpolate(ibx_plan* plan, void* stream);
 /* Status of the marker data seen by the last ibx_plan_bin (synchronises
  * the stream, then clears the word): IBX_OK, IBX_E_NONFINITE (a position
  * was NaN or infinite; that marker was skipped), IBX_E_TOO_LARGE (a list
- * capacity overflowed) or IBX_E_TIMEOUT (a bounded wait for a staged copy
- * gave up; the interpolated values are incomplete). */
+ * capacity overflowed) or IBX_E_TIMEOUT (a bounded wait gave up: for a
+ * staged copy, the interpolated values are incomplete; in step mode 2, for
+ * the dense spread, the per-visit spread went ahead without it). */
 int ibx_plan_status(ibx_plan* plan, void* stream, int* status);
 /* Copy the binning of the last ibx_plan_bin to host arrays (any may be
  * NULL; synchronises the device).  Markers are numbered across problems in
@@ -381,7 +382,16 @@ int ibx_plan_get_interp_kernel(const ibx_plan* plan);
  * reference counterpart; chosen by the autotuner): 1 = concurrently, the
  * interpolation on a stream of the plan forked from and joined back to the
  * caller's stream (default); 0 = one after the other on the caller's
- * stream.  Same results. */
+ * stream; 2 = both in one persistent launch on the caller's stream, whose
+ * blocks take the dense spread's work items, the interpolation of the same
+ * items, the interpolation of the other markers and then the per-visit
+ * spread of the tiles from one work counter (the interpolation form and the
+ * per-visit form set by ibx_plan_set_interp_kernel / _visit_kernel do not
+ * apply: it runs forms 1 and 2).  Same results: the interpolation bit for
+ * bit, the spread to rounding (its atomic additions come in another order).
+ * The per-visit spread of mode 2 waits, at most about a second, for the
+ * dense spread of every tile to finish; a wait that runs out is reported
+ * by ibx_plan_status as IBX_E_TIMEOUT. */
 int ibx_plan_set_step_mode(ibx_plan* plan, int mode);
 int ibx_plan_get_step_mode(const ibx_plan* plan);
 /* Most markers per home unit (1..32; no reference counterpart; chosen by the

@@ -361,7 +361,7 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1])
+@pytest.mark.parametrize("step_mode", [0, 1, 2])
 @pytest.mark.parametrize("interp_form", [0, 1, 2, 3, 4])
 def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_form, step_mode):
     """ibx_plan_step (spread and interpolation on two streams, or one after
@@ -394,6 +394,61 @@ def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_for
         assert cases.rel_err(f, f_ref) <= MIXED_TOL
         assert cases.rel_err(U_t.double().cpu().numpy(), U_ref) <= MIXED_TOL
     assert plan.status() == ibx.OK
+    plan.close()
+
+
+@pytest.mark.parametrize("tile_shape", [0, 1])
+@pytest.mark.parametrize("dense_min", [None, 0, 1 << 30])
+@pytest.mark.parametrize("kernel", KERNEL_NAMES)
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("centering,depth", [(1, 1), (0, 3)])
+def test_fused_step_matches_oracle_and_separate_launches(ibx, oracle, kernel, dim, centering, depth, tile_shape,
+                                                         dense_min):
+    """Step mode 2 (spread and interpolation of the binned markers in one
+    persistent launch) against the oracle, step after step, and its
+    interpolation bit-identical to the separate launches (step mode 0)."""
+    rng = np.random.default_rng(131 + dim + 10 * centering + 100 * KERNEL_NAMES.index(kernel) + tile_shape)
+    N = [26, 21, 18][:dim] if dim == 3 else [44, 37]
+    n = 3000
+    X = seam_markers(rng, n, dim)
+    ncomp = dim if centering == 1 else depth
+    F = rng.standard_normal(n * ncomp)
+    u = rng.standard_normal([ncomp] + list(N)[::-1])
+    f_ref, U_ref = oracle.periodic_problem(dim, N, kernel, X, F=F, u=u, centering=centering, depth=depth)
+    shape = list(N)[::-1]
+    X_t = torch.tensor(X, device="cuda")
+    if centering == ibx.SIDE:
+        f_t = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(dim)]
+        u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    else:
+        f_t = torch.zeros([depth] + shape, dtype=torch.float32, device="cuda")
+        u_t = torch.tensor(u, dtype=torch.float32, device="cuda")
+    F_t = torch.tensor(F, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * ncomp, dtype=torch.float32, device="cuda")
+    mk = lambda q, Q: ibx.make_problem(dim, centering, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q,
+                                       q_depth=1 if centering else depth, Q_depth=ncomp)
+    plan = ibx.Plan(mk(f_t, F_t), kernel, ibx.MIXED, interp_problems=[mk(u_t, U_t)], tile_shape=tile_shape)
+    if dense_min is not None:
+        plan.set_tuning(dense_min=dense_min)
+    got = {}
+    for mode in (0, 2, 2):
+        plan.step_mode = mode
+        assert plan.step_mode == mode
+        for t in (f_t if centering == ibx.SIDE else [f_t]):
+            t.zero_()
+        U_t.zero_()
+        plan.step()
+        torch.cuda.synchronize()
+        assert plan.status() == ibx.OK
+        f = np.stack([t.double().cpu().numpy() for t in f_t]) if centering == ibx.SIDE else f_t.double().cpu().numpy()
+        U = U_t.double().cpu().numpy()
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL
+        assert cases.rel_err(U, U_ref) <= MIXED_TOL
+        if mode in got:
+            assert np.array_equal(U, got[mode])
+        got[mode] = U
+    assert np.array_equal(got[0], got[2])
     plan.close()
 
 
