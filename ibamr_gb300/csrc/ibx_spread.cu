@@ -818,9 +818,10 @@ put_weights(float* dst, const float* w, int b, int N, int org)
 // grid narrower than the stencil wraps two points onto one cell); 1: each
 // vector is assembled in registers (a compare and select per tile position
 // and stencil point) and written with 16-byte stores, no zeroing (form 3:
-// fewer shared-memory wavefronts, more arithmetic).  The grid values are read
-// through L2 only (each is read once).
-template <int DIM, int K, int SH, int PREP>
+// fewer shared-memory wavefronts, more arithmetic).  L2ONLY: the grid values
+// are read past L1 (the fused step, where atomics of the same launch wrote
+// them).
+template <int DIM, int K, int SH, int PREP, bool L2ONLY = false>
 __device__ __forceinline__ void
 gather_tile(const DevPlan& D, int t, float* slots, int lane)
 {
@@ -969,7 +970,8 @@ gather_tile(const DevPlan& D, int t, float* slots, int lane)
                         continue;
                     if (vec)
                     {
-                        float4 v = __ldcg(reinterpret_cast<const float4*>(q + o + i));
+                        float4 v = L2ONLY ? __ldcg(reinterpret_cast<const float4*>(q + o + i))
+                                          : *reinterpret_cast<const float4*>(q + o + i);
                         v.x = merge3(v.x, h[0], l[0]);
                         v.y = merge3(v.y, h[1], l[1]);
                         v.z = merge3(v.z, h[2], l[2]);
@@ -981,7 +983,7 @@ gather_tile(const DevPlan& D, int t, float* slots, int lane)
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
                             if (x0 + i + e < P.N[0] && (h[e] != 0.f || l[e] != 0.f))
-                                q[o + i + e] = merge3(__ldcg(q + o + i + e), h[e], l[e]);
+                                q[o + i + e] = merge3(L2ONLY ? __ldcg(q + o + i + e) : q[o + i + e], h[e], l[e]);
                     }
                 }
             }
@@ -1084,7 +1086,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 3) step_fused(const DevPlan D)
             }
             __syncthreads();
             const int t = (w - nD - nU - nC) * GATHER_WARPS + warp;
-            if (t < D.n_tiles) gather_tile<DIM, K, SH, PREP>(D, t, sm + warp * 32 * GL::SS, lane);
+            if (t < D.n_tiles) gather_tile<DIM, K, SH, PREP, true>(D, t, sm + warp * 32 * GL::SS, lane);
         }
     }
 }
