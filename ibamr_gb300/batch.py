@@ -112,24 +112,35 @@ class BatchedProblems:
         return buf[a:b]
 
     # -- stepping ----------------------------------------------------------
-    def step(self):
+    def step(self, io=None):
         """bin, then spread (f += S F) and interpolate (U = S* u)
-        concurrently, eagerly."""
-        self.plan.step()
+        concurrently, eagerly.  io: host transfers around the step, a dict of
+        Plan.step_io's in_X / in_Q / out_Q lists of (dst, src) pairs."""
+        if io:
+            self.plan.step_io(**io)
+        else:
+            self.plan.step()
 
-    def capture(self):
-        """Capture one step into a CUDA graph (after an eager warm-up step)."""
+    def host_io(self, Xh, Fh, Uh):
+        """The transfers of a step whose positions Xh and forces Fh come from
+        pinned host tensors and whose velocities go to the pinned host tensor
+        Uh (all batch-wide, the layout of X, F and U)."""
+        return dict(in_X=[(self.X, Xh)], in_Q=[(self.F, Fh)], out_Q=[(Uh, self.U)])
+
+    def capture(self, io=None):
+        """Capture one step (with the host transfers io, see step) into a
+        CUDA graph, after an eager warm-up step."""
         import torch
 
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
-            self.step()
+            self.step(io)
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.step()
+            self.step(io)
         self.graph = g
         return g
 

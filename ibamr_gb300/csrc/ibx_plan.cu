@@ -158,6 +158,11 @@ struct ibx_plan
     // the caller's stream (0)
     cudaStream_t side, spread_s;
     cudaEvent_t ev_fork, ev_join, ev_join2;
+    // ibx_plan_step_io: the spread values' upload runs on `up`, behind the
+    // positions' upload on the caller's stream (ev_x), and the spread waits
+    // for it (ev_q)
+    cudaStream_t up;
+    cudaEvent_t ev_x, ev_q;
     int step_mode;
     int n_tma; // problems whose interpolation sources have tensor maps
 };
@@ -332,7 +337,10 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         cudaStreamCreateWithPriority(&plan->spread_s, cudaStreamNonBlocking, greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&plan->ev_join2, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&plan->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&plan->up, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_x, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_q, cudaEventDisableTiming) != cudaSuccess)
     {
         cudaFree(dmem);
         delete plan;
@@ -356,40 +364,136 @@ ibx_plan_bin(ibx_plan* plan, void* stream)
     return ibx::bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, static_cast<cudaStream_t>(stream));
 }
 
+} // extern "C"
+
+namespace
+{
+bool
+transfers_ok(const ibx_transfer* t, int n)
+{
+    if (n < 0 || (n > 0 && !t)) return false;
+    for (int i = 0; i < n; ++i)
+        if (t[i].bytes > 0 && (!t[i].dst || !t[i].src)) return false;
+    return true;
+}
+
 int
-ibx_plan_step(ibx_plan* plan, void* stream)
+copy_all(const ibx_transfer* t, int n, cudaStream_t s)
+{
+    for (int i = 0; i < n; ++i)
+        if (t[i].bytes > 0 && cudaMemcpyAsync(t[i].dst, t[i].src, t[i].bytes, cudaMemcpyDefault, s) != cudaSuccess)
+            return IBX_E_CUDA;
+    return IBX_OK;
+}
+
+// One step with its transfers: positions in on s; spread values in on `up`
+// behind them; binning on s; spread and interpolation by the step mode, the
+// spread after the spread values; interpolated values out after the
+// interpolation.  Every stream of the plan is joined back into s, also after
+// a failure, so that a capture in progress stays valid.
+int
+plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
+          const ibx_transfer* out_Q, int n_out_Q)
 {
     using namespace ibx;
-    if (!plan) return IBX_E_ARG;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc = copy_all(in_X, n_in_X, s);
+    if (rc) return rc;
+    bool up = false;
+    for (int i = 0; i < n_in_Q; ++i) up = up || in_Q[i].bytes > 0;
+    if (up)
+    {
+        if (cudaEventRecord(plan->ev_x, s) != cudaSuccess || cudaStreamWaitEvent(plan->up, plan->ev_x, 0) != cudaSuccess)
+            return IBX_E_CUDA;
+        rc = copy_all(in_Q, n_in_Q, plan->up);
+        if (cudaEventRecord(plan->ev_q, plan->up) != cudaSuccess) return IBX_E_CUDA;
+        if (rc)
+            return cudaStreamWaitEvent(s, plan->ev_q, 0) == cudaSuccess ? rc : IBX_E_CUDA;
+    }
+    // joins the upload into `st` (the stream the spread runs on)
+    auto wait_up = [&](cudaStream_t st) { return !up || cudaStreamWaitEvent(st, plan->ev_q, 0) == cudaSuccess; };
     // Interpolation in marker order needs only the stencil records: in the
     // concurrent mode it forks as soon as they exist, beside the counting
     // sort; the other forms fork after the whole binning.
     const bool early = plan->step_mode == 1 && plan->D.interp_form == 2;
-    int rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr);
-    if (rc) return rc;
+    rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr);
+    if (rc) return wait_up(s) ? rc : IBX_E_CUDA;
+    bool out = false;
+    for (int i = 0; i < n_out_Q; ++i) out = out || out_Q[i].bytes > 0;
+    if (plan->step_mode == 2)
+    {
+        if (!wait_up(s)) return IBX_E_CUDA;
+        rc = launch_fused(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
+        return rc ? rc : copy_all(out_Q, n_out_Q, s);
+    }
     if (plan->step_mode == 0)
     {
-        rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
-        return rc ? rc : launch_interp(plan->dim, plan->kernel, plan->D, s);
+        // the interpolation first, its values copied out on `side` while the
+        // spread runs
+        rc = launch_interp(plan->dim, plan->kernel, plan->D, s);
+        bool forked = false;
+        if (!rc && out)
+        {
+            if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess ||
+                cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
+                rc = IBX_E_CUDA;
+            else
+            {
+                forked = true;
+                rc = copy_all(out_Q, n_out_Q, plan->side);
+            }
+        }
+        if (!wait_up(s)) rc = rc ? rc : IBX_E_CUDA;
+        if (!rc) rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
+        if (forked && (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
+                       cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess))
+            rc = rc ? rc : IBX_E_CUDA;
+        return rc;
     }
-    if (plan->step_mode == 2) return launch_fused(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
     // spread and interpolation read the same records and write different
-    // arrays: they overlap on the device, the spread's blocks dispatched first
+    // arrays: they overlap on the device.  The longer phase, the spread, runs
+    // on the stream of greatest priority -- unless the interpolated values
+    // are copied out, then the interpolation does, so that the copy runs
+    // beside the rest of the spread instead of after it.
+    cudaStream_t s_int = out ? plan->spread_s : plan->side;
+    cudaStream_t s_spr = out ? plan->side : plan->spread_s;
     if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
-        cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
+        cudaStreamWaitEvent(s_int, plan->ev_fork, 0) != cudaSuccess)
+        return wait_up(s) ? IBX_E_CUDA : IBX_E_CUDA;
+    if ((early && cudaEventRecord(plan->ev_join2, s) != cudaSuccess) || // the whole binning
+        cudaStreamWaitEvent(s_spr, early ? plan->ev_join2 : plan->ev_fork, 0) != cudaSuccess || !wait_up(s_spr))
+    {
+        // join the forked interpolation stream and the upload before failing
+        if (cudaEventRecord(plan->ev_join, s_int) == cudaSuccess) cudaStreamWaitEvent(s, plan->ev_join, 0);
+        wait_up(s);
         return IBX_E_CUDA;
-    if (early && cudaEventRecord(plan->ev_join2, s) != cudaSuccess) return IBX_E_CUDA; // the whole binning
-    if (cudaStreamWaitEvent(plan->spread_s, early ? plan->ev_join2 : plan->ev_fork, 0) != cudaSuccess)
-        return IBX_E_CUDA;
-    rc = launch_interp(plan->dim, plan->kernel, plan->D, plan->side);
-    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, plan->spread_s);
+    }
+    rc = launch_interp(plan->dim, plan->kernel, plan->D, s_int);
+    if (!rc) rc = copy_all(out_Q, n_out_Q, s_int);
+    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s_spr);
     // join even after a failed launch, so that no stream of the plan is left forked
-    if (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
-        cudaEventRecord(plan->ev_join2, plan->spread_s) != cudaSuccess ||
+    if (cudaEventRecord(plan->ev_join, s_int) != cudaSuccess || cudaEventRecord(plan->ev_join2, s_spr) != cudaSuccess ||
         cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess || cudaStreamWaitEvent(s, plan->ev_join2, 0) != cudaSuccess)
         return IBX_E_CUDA;
     return rc ? rc : rs;
+}
+} // namespace
+
+extern "C" {
+
+int
+ibx_plan_step(ibx_plan* plan, void* stream)
+{
+    if (!plan) return IBX_E_ARG;
+    return plan_step(plan, static_cast<cudaStream_t>(stream), nullptr, 0, nullptr, 0, nullptr, 0);
+}
+
+int
+ibx_plan_step_io(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
+                 const ibx_transfer* out_Q, int n_out_Q, void* stream)
+{
+    if (!plan || !transfers_ok(in_X, n_in_X) || !transfers_ok(in_Q, n_in_Q) || !transfers_ok(out_Q, n_out_Q))
+        return IBX_E_ARG;
+    return plan_step(plan, static_cast<cudaStream_t>(stream), in_X, n_in_X, in_Q, n_in_Q, out_Q, n_out_Q);
 }
 
 int
@@ -561,11 +665,15 @@ ibx_plan_destroy(ibx_plan* plan)
     if (!plan) return IBX_OK;
     cudaStreamSynchronize(plan->side);
     cudaStreamSynchronize(plan->spread_s);
+    cudaStreamSynchronize(plan->up);
     cudaStreamDestroy(plan->side);
     cudaStreamDestroy(plan->spread_s);
+    cudaStreamDestroy(plan->up);
     cudaEventDestroy(plan->ev_fork);
     cudaEventDestroy(plan->ev_join);
     cudaEventDestroy(plan->ev_join2);
+    cudaEventDestroy(plan->ev_x);
+    cudaEventDestroy(plan->ev_q);
     const cudaError_t e = cudaFree(plan->dmem);
     delete plan;
     return e == cudaSuccess ? IBX_OK : IBX_E_CUDA;

@@ -88,6 +88,9 @@ def lib():
             L.ibx_plan_tile_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
             for name in ("ibx_plan_bin", "ibx_plan_spread", "ibx_plan_interpolate", "ibx_plan_step"):
                 getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            T = ctypes.POINTER(Transfer)
+            L.ibx_plan_step_io.argtypes = [ctypes.c_void_p, T, ctypes.c_int, T, ctypes.c_int, T, ctypes.c_int,
+                                           ctypes.c_void_p]
             L.ibx_plan_tma_problems.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.restype = ctypes.c_longlong
@@ -373,6 +376,25 @@ def fill_ghosts(problem, periodic, stream=None):
         raise IbxError(rc, "ibx_fill_ghosts")
 
 
+class Transfer(ctypes.Structure):
+    """ibx_transfer: one copy of ibx_plan_step_io."""
+    _fields_ = [("dst", ctypes.c_void_p), ("src", ctypes.c_void_p), ("bytes", ctypes.c_size_t)]
+
+
+def _transfers(pairs):
+    """ctypes array of ibx_transfer for (dst, src) tensor pairs."""
+    pairs = list(pairs)
+    if not pairs:
+        return None
+    arr = (Transfer * len(pairs))()
+    for k, (dst, src) in enumerate(pairs):
+        nb = dst.numel() * dst.element_size()
+        if src.numel() * src.element_size() != nb or not dst.is_contiguous() or not src.is_contiguous():
+            raise ValueError("a transfer needs two contiguous tensors of the same byte size")
+        arr[k] = Transfer(dst.data_ptr(), src.data_ptr(), nb)
+    return arr
+
+
 class Plan:
     """Binned spread/interpolate pipeline over fixed IBX_MODE_PERIODIC problems."""
 
@@ -410,6 +432,18 @@ class Plan:
         rc = lib().ibx_plan_step(self.h, _stream_handle(stream))
         if rc:
             raise IbxError(rc, "ibx_plan_step")
+
+    def step_io(self, in_X=(), in_Q=(), out_Q=(), stream=None):
+        """One step with its host transfers (ibx_plan_step_io): each argument
+        a list of (dst, src) tensor pairs of equal byte size -- in_X copied
+        first, in_Q behind it beside the binning (the spread waits for it),
+        out_Q as soon as the interpolation ends.  Host tensors should be
+        pinned."""
+        arrs = [_transfers(pairs) for pairs in (in_X, in_Q, out_Q)]
+        rc = lib().ibx_plan_step_io(self.h, arrs[0], len(in_X), arrs[1], len(in_Q), arrs[2], len(out_Q),
+                                    _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_plan_step_io")
 
     def spread(self, stream=None):
         rc = lib().ibx_plan_spread(self.h, _stream_handle(stream))

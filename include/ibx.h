@@ -17,6 +17,8 @@
 #ifndef IBX_H
 #define IBX_H
 
+#include <stddef.h> /* size_t */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -319,6 +321,28 @@ int ibx_plan_bin(ibx_plan* plan, void* stream);
  * the least, so the longer phase gets the SMs first), both joined back into
  * `stream` before the call's work ends.  Graph-capturable like the others. */
 int ibx_plan_step(ibx_plan* plan, void* stream);
+/* One copy of ibx_plan_step_io: `bytes` bytes from src to dst, either of
+ * them host or device memory (cudaMemcpyDefault).  Host buffers must be
+ * page-locked for the copies to run beside the kernels (and for the call to
+ * be captured in a CUDA graph). */
+typedef struct ibx_transfer
+{
+    void* dst;
+    const void* src;
+    size_t bytes;
+} ibx_transfer;
+/* ibx_plan_step with the step's host transfers ordered around it, for a
+ * caller whose marker data live in host memory (no reference counterpart:
+ * the reference's LData are host arrays, which this call moves in and out).
+ * in_X (positions) are copied first, on `stream`; in_Q (the values to
+ * spread) on a stream of the plan behind them, beside the binning, and the
+ * spread waits for them; out_Q (the interpolated values) are copied as soon
+ * as the interpolation ends, beside the rest of the spread (with out_Q the
+ * concurrent mode gives the interpolation the greater stream priority, so
+ * that it ends first).  Any count may be 0.  Everything is joined back into `stream` (also after a failure);
+ * graph-capturable with page-locked host buffers. */
+int ibx_plan_step_io(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
+                     const ibx_transfer* out_Q, int n_out_Q, void* stream);
 int ibx_plan_spread(ibx_plan* plan, void* stream);
 int ibx_plan_interpolate(ibx_plan* plan, void* stream);
 /* Status of the marker data seen by the last ibx_plan_bin (synchronises
@@ -382,7 +406,7 @@ int ibx_plan_get_interp_kernel(const ibx_plan* plan);
  * reference counterpart; chosen by the autotuner): 1 = concurrently, the
  * interpolation on a stream of the plan forked from and joined back to the
  * caller's stream (default); 0 = one after the other on the caller's
- * stream; 2 = both in one persistent launch on the caller's stream, whose
+ * stream, the interpolation first; 2 = both in one persistent launch on the caller's stream, whose
  * blocks take the dense spread's work items, the interpolation of the same
  * items, the interpolation of the other markers and then the per-visit
  * spread of the tiles from one work counter (the interpolation form and the

@@ -68,6 +68,8 @@ def test_plan_knobs_reject_a_null_plan(libibx):
         assert fn(None) == -1, getter
     L.ibx_plan_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     assert L.ibx_plan_set_tuning(None, 128, 32, 2) == E_ARG
+    L.ibx_plan_step_io.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p, ctypes.c_int] * 3 + [ctypes.c_void_p]
+    assert L.ibx_plan_step_io(None, None, 0, None, 0, None, 0, None) == E_ARG
 
 
 def test_host_queries(libibx):

@@ -452,6 +452,67 @@ def test_fused_step_matches_oracle_and_separate_launches(ibx, oracle, kernel, di
     plan.close()
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("step_mode", [0, 1, 2])
+@pytest.mark.parametrize("interp_form", [1, 2])
+def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, interp_form):
+    """ibx_plan_step_io moves positions and forces in from pinned host memory
+    and the interpolated values out: the oracle's answer eagerly, and from a
+    CUDA graph of the call replayed with new host forces and positions."""
+    rng = np.random.default_rng(151 + dim + 3 * step_mode)
+    N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
+    n = 2500
+    X = seam_markers(rng, n, dim)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    X_t = torch.full((n * dim,), 0.5, dtype=torch.float64, device="cuda")
+    f_t = [torch.zeros(list(N)[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    F_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    Xh = torch.tensor(X).pin_memory()
+    Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
+    Uh = torch.zeros(n * dim, dtype=torch.float32).pin_memory()
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), "IB_4", ibx.MIXED, interp_problems=[mk(u_t, U_t)])
+    plan.interp_kernel = interp_form
+    plan.step_mode = step_mode
+    io = dict(in_X=[(X_t, Xh)], in_Q=[(F_t, Fh)], out_Q=[(Uh, U_t)])
+
+    def check(Xc, Fc):
+        f_ref, U_ref = oracle.periodic_problem(dim, N, "IB_4", Xc, F=Fc, u=u, centering=1)
+        f = np.stack([t.double().cpu().numpy() for t in f_t])
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL
+        assert cases.rel_err(Uh.double().numpy(), U_ref) <= MIXED_TOL
+
+    plan.step_io(**io)
+    torch.cuda.synchronize()
+    assert plan.status() == ibx.OK
+    check(X, F)
+    # captured: the graph reads the host buffers at every replay
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.step_io(**io, stream=s)
+    for rep in range(2):
+        X2 = seam_markers(rng, n, dim)
+        F2 = rng.standard_normal(n * dim)
+        Xh.copy_(torch.tensor(X2))
+        Fh.copy_(torch.tensor(F2, dtype=torch.float32))
+        Uh.zero_()
+        for t in f_t:
+            t.zero_()
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert plan.status() == ibx.OK
+        check(X2, F2)
+    del g
+    plan.close()
+
+
 @pytest.mark.parametrize("form", [1, 2, 3])
 @pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
