@@ -11,8 +11,9 @@ the same workload, the error against it, the CPU baseline, the end-to-end
 rate with host buffers and the roofline of the dominant kernel are reported
 on the same JSON line, and nested objects carry the other measured
 configurations: ``ib6`` (the same workload with IB_6), ``batched`` (512
-independent 2D problems, one CUDA graph per step, autotuned) and ``serving``
-(Poisson request stream over resident simulations, p50/p99 latency).
+independent 2D problems, one CUDA graph per step, autotuned), ``serving``
+(Poisson request stream over resident simulations, p50/p99 latency) and
+``fortran_abi`` (the reference's Fortran entry points with host arrays).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                   [--workload all|helices|batched|serving] [--kernel K]
@@ -750,6 +751,64 @@ def nested(line):
     return {k: line[k] for k in NESTED_KEYS if k in line}
 
 
+def fortran_abi_case(dev, reps=5):
+    """The reference's own entry points, called as LEInteractor calls them:
+    lagrangian_ib_4_spread3d_ and lagrangian_ib_4_interp3d_ (the Fortran ABI
+    of libibx) on one ghosted 128^3 cell patch of depth 3 with 200,000
+    markers, every array a host array (staged through the library's pool,
+    copied in and back per call), against the same calls with device
+    arrays.  One step = one spread + one interpolation."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from ibamr_gb300 import ibx
+
+    L = ibx.lib()
+    n, N, g, depth = 200_000, 128, 3, 3
+    rng = np.random.default_rng(5)
+    X = rng.uniform(0.0, 1.0, (n, 3)).reshape(-1)
+    V = rng.standard_normal(n * depth)
+    u = np.zeros(depth * (N + 2 * g) ** 3)
+    idx = np.arange(n, dtype=np.int32)
+    sh = np.zeros(3 * n)
+    dx = np.full(3, 1.0 / N)
+    xl, xu = np.zeros(3), np.ones(3)
+    ri = lambda v: ctypes.byref(ctypes.c_int(int(v)))
+    box = [ri(0), ri(N - 1)] * 3
+    gw = [ri(g)] * 3
+
+    def pt(a):
+        return ctypes.c_void_p(a.data_ptr()) if isinstance(a, torch.Tensor) else a.ctypes.data_as(ctypes.c_void_p)
+
+    def step(arrs):
+        uu, XX, VV, ii, ss = arrs
+        L.lagrangian_ib_4_spread3d_(pt(dx), pt(xl), pt(xu), ri(depth), pt(ii), pt(ss), ri(n), pt(XX), pt(VV),
+                                    *box, *gw, pt(uu))
+        L.lagrangian_ib_4_interp3d_(pt(dx), pt(xl), pt(xu), ri(depth), *box, *gw, pt(uu), pt(ii), pt(ss), ri(n),
+                                    pt(XX), pt(VV))
+
+    def wall(arrs):
+        step(arrs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            step(arrs)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    host = (u, X, V.copy(), idx, sh)
+    devs = tuple(torch.tensor(a, device=dev) for a in host)
+    ms_h = wall(host)
+    ms_d = wall(devs)
+    return {"call": "lagrangian_ib_4_spread3d_ + lagrangian_ib_4_interp3d_", "markers": n,
+            "patch": "128^3 cells, ghost width 3, depth 3, FP64", "host_arrays_ms": ms_h, "device_arrays_ms": ms_d,
+            "host_arrays_markers_per_s": n / (ms_h * 1e-3), "device_arrays_markers_per_s": n / (ms_d * 1e-3),
+            # spread: u in and out, X, V, indices, shifts in; interpolation: u, X, V, indices, shifts in, V out
+            "host_bytes_per_step": int(8 * (3 * u.size + 2 * X.size + 3 * V.size + 2 * sh.size) + 4 * 2 * idx.size)}
+
+
 def run_ours(args):
     import torch
 
@@ -783,6 +842,7 @@ def run_ours(args):
                                               args.warmup))
             line["batched"] = nested(batched_case(args, dev, world, with_cpu, args.steps, args.warmup))
             line["serving"] = nested(serving_case(args, dev, world, with_cpu, args.steps))
+            line["fortran_abi"] = fortran_abi_case(dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -10,6 +10,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace ibx
@@ -204,6 +205,57 @@ run_generic(const ibx_problem* problems, int n_problems, int kernel, int precisi
 } // namespace
 } // namespace ibx
 
+namespace ibx
+{
+namespace
+{
+constexpr int MAX_DEVICES = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[MAX_DEVICES] = {};
+
+cudaMemPool_t
+staging_pool()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pools[dev])
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+        // keep freed memory in the pool for the next call
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+} // namespace
+
+void*
+staging_alloc(size_t bytes)
+{
+    cudaMemPool_t pool = staging_pool();
+    void* p = nullptr;
+    if (!pool || cudaMallocFromPoolAsync(&p, bytes, pool, nullptr) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void
+staging_free(void* p)
+{
+    if (p) cudaFreeAsync(p, nullptr);
+}
+} // namespace ibx
+
 extern "C" {
 
 int
@@ -278,13 +330,16 @@ ibx_device_alloc(void** ptr, long long bytes)
     if (!ptr || bytes < 0) return IBX_E_ARG;
     *ptr = nullptr;
     if (bytes == 0) return IBX_OK;
-    return cudaMalloc(ptr, (size_t)bytes) == cudaSuccess ? IBX_OK : IBX_E_OOM;
+    *ptr = ibx::staging_alloc((size_t)bytes);
+    return *ptr ? IBX_OK : IBX_E_OOM;
 }
 
 int
 ibx_device_free(void* ptr)
 {
-    return cudaFree(ptr) == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+    if (!ptr) return IBX_OK;
+    ibx::staging_free(ptr);
+    return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 int

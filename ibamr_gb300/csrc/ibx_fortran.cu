@@ -33,7 +33,8 @@ on_device(const void* p)
 }
 
 // A caller array made available on the device: used in place when it is
-// device memory, else copied into a temporary buffer (and back on request).
+// device memory, else copied into a buffer of the library's staging pool
+// (and back on request).
 struct Staged
 {
     void* host = nullptr;
@@ -52,7 +53,8 @@ struct Staged
             dev = host;
             return;
         }
-        if (cudaMalloc(&dev, n) != cudaSuccess) die(routine, "device allocation failed");
+        dev = ibx::staging_alloc(n);
+        if (!dev) die(routine, "device allocation failed");
         owned = true;
         if (copy_in && cudaMemcpy(dev, p, n, cudaMemcpyHostToDevice) != cudaSuccess) die(routine, "copy to the device failed");
     }
@@ -64,7 +66,7 @@ struct Staged
     }
     ~Staged()
     {
-        if (owned) cudaFree(dev);
+        if (owned) ibx::staging_free(dev);
     }
 };
 

@@ -274,9 +274,13 @@ int ibx_spring_forces(int dim, int n_markers, const double* X, int n_springs, co
                       int* status, void* stream);
 
 /* ---- host helpers (used by the C++ LEInteractor layer) ----------------- */
-/* Device memory and copies for callers without the CUDA runtime headers:
- * cudaMalloc / cudaFree / blocking cudaMemcpy (to_device != 0: host to
- * device) / cudaDeviceSynchronize. */
+/* Device memory and copies for callers without the CUDA runtime headers.
+ * ibx_device_alloc / ibx_device_free take buffers from a memory pool of the
+ * library that keeps freed memory for the next allocation (no cudaMalloc /
+ * cudaFree per call); both are ordered on the legacy default stream, so work
+ * on non-blocking streams that uses a buffer must be synchronised before it
+ * is freed.  ibx_memcpy is a blocking cudaMemcpy (to_device != 0: host to
+ * device); ibx_synchronize is cudaDeviceSynchronize. */
 int ibx_device_alloc(void** ptr, long long bytes);
 int ibx_device_free(void* ptr);
 int ibx_memcpy(void* dst, const void* src, long long bytes, int to_device);
