@@ -322,6 +322,30 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # Helices workload (the headline configuration, and IB_6)
 # ---------------------------------------------------------------------------
+# FP64 rate of a GB300 (nominal, non-tensor), for the FP64 floor of a step
+GB300_FP64_TFLOPS = 1.25
+
+
+def fp64_fma_floor_ms(n_markers, dim, width):
+    """Time the multiply-adds of one spread + interpolation in FP64 take at
+    the GB300's nominal FP64 rate: dim components x width^dim stencil points
+    per marker, one FMA each way -- a floor for any FP64 form of the step."""
+    fmas = 2 * n_markers * dim * width ** dim
+    return 2 * fmas / (GB300_FP64_TFLOPS * 1e12) * 1e3
+
+
+def tile_index(X, N, edges):
+    """Tile of each marker's cell (periodic unit box, N cells per side)."""
+    P = np.asarray(X).reshape(-1, len(N))
+    t = np.zeros(len(P), dtype=np.int64)
+    stride = 1
+    for d in range(len(N)):
+        c = np.floor(P[:, d] * N[d]).astype(np.int64) % N[d]
+        t += (c // edges[d]) * stride
+        stride *= (N[d] + edges[d] - 1) // edges[d]
+    return t
+
+
 def pick_io_mode(plan, step_e2e, timed, steps, recapture=None):
     """Step mode of the end-to-end step (bin + spread + interpolate with
     their host transfers): the plan's own mode, or mode 0 (interpolation
@@ -481,7 +505,19 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
 
     step_plain()
     ms_plain = timed(step_plain, max(2, steps // 5))
-    del fd, ud, Fd, Ud
+    # the same form over the markers sorted into tile order once, outside the
+    # timed region (the locality a binning gives the marker-parallel form)
+    order = np.argsort(tile_index(X, [N[0]] * 3, plan.tile_shape[1]), kind="stable")
+    X_s = torch.tensor(X.reshape(-1, 3)[order].reshape(-1), device=dev)
+    F_s = torch.tensor(F.reshape(-1, 3)[order].reshape(-1), device=dev)
+
+    def step_plain_sorted():
+        ibx.spread(prob(fd, X_s, F_s), kernel, ibx.FP64)
+        ibx.interpolate(prob(ud, X_s, Ud), kernel, ibx.FP64)
+
+    step_plain_sorted()
+    ms_plain_sorted = timed(step_plain_sorted, max(2, steps // 5))
+    del fd, ud, Fd, Ud, X_s, F_s
 
     # end to end through the C ABI with host buffers (ibx_plan_step_io): the
     # positions go up first, the forces behind them beside the binning (which
@@ -523,7 +559,9 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
                    "precision": "mixed", "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
-        "plain_fp64": {"value": world * n / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+        "plain_fp64": {"value": world * n / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                       "tile_order_ms_per_step": ms_plain_sorted,
+                       "fp64_fma_floor_ms": fp64_fma_floor_ms(n, 3, KERNEL_WIDTHS[kernel])},
         "mixed_vs_plain": ms_plain / ms,
         "error_vs_fp64": {"spread": err_f, "interpolate": err_U, "tolerance": 1e-5},
         "status": ibx.status_string(status),
