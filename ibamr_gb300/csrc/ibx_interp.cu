@@ -11,6 +11,9 @@
 //    ones (form 1), or every marker in the caller's order (form 2: it needs
 //    only the stencil records, so the step can start it before the counting
 //    sort; fibre markers given in fibre order share runs as in home order).
+//    In form 1 the sparse-homed markers, which seldom share a stencil, go
+//    to interp_chunks_sparse: the same sums without the register cache, in
+//    80 registers instead of 128 (24 resident warps per SM instead of 16).
 //  - interp_units (form 1, dense-homed): the work items of the dense spread
 //    (item_units home units of one tile); a group of lanes per (unit,
 //    component), the footprint's z-planes split over the group, loads the
@@ -30,11 +33,19 @@ namespace ibx
 namespace
 {
 // Chunks of consecutive home-order markers, one component per thread
-// (chunk_body), the stencil values cached in registers across a run.
+// (chunk_body), the stencil values cached in registers across a run; or,
+// for the sparse-homed markers alone (which seldom share a stencil), read
+// as they are summed, in fewer registers (more resident warps).
 template <int DIM, int K>
 __global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D, int select, int marker_order)
 {
     chunk_body<DIM, K, true>(D, blockIdx.x * (long long)blockDim.x + threadIdx.x, select, marker_order);
+}
+
+template <int DIM, int K>
+__global__ void __launch_bounds__(INTERP_THREADS, 3) interp_chunks_sparse(const DevPlan D)
+{
+    chunk_body<DIM, K, false>(D, blockIdx.x * (long long)blockDim.x + threadIdx.x, SEL_SPARSE, 0);
 }
 
 // Dense-homed markers by home unit (units_item); items are taken from a
@@ -384,7 +395,10 @@ launch_interp_k(const DevPlan& D, cudaStream_t s)
     const long long chunks = (D.n_markers + CHUNK - 1) / CHUNK;
     const unsigned bx = (unsigned)((chunks * D.max_ncomp + INTERP_THREADS - 1) / INTERP_THREADS);
     if (bx == 0) return IBX_OK;
-    interp_chunks<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D, units ? SEL_SPARSE : SEL_ALL, D.interp_form == 2);
+    if (units)
+        interp_chunks_sparse<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D);
+    else
+        interp_chunks<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D, SEL_ALL, D.interp_form == 2);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }

@@ -256,10 +256,22 @@ units_item(const DevPlan& D, int item, int* s_order, int* s_start)
                                 __ldg(q + (DIM == 3 ? cz * n01 : 0) + co[1][i1] * n0 + co[0][i0]);
                 }
             }
-            for (int v = un.x; v < un.x + un.y; ++v)
+            // Markers of the unit, software-pipelined: the next marker's
+            // record and id are loaded before the current marker's arithmetic.
+            const int vend = un.x + un.y;
+            Rec Rn = D.hrec[un.x];
+            int gn = D.home_list[un.x];
+            for (int v = un.x; v < vend; ++v)
             {
+                const Rec R = Rn;
+                const int g = gn;
+                if (v + 1 < vend)
+                {
+                    Rn = D.hrec[v + 1];
+                    gn = D.home_list[v + 1];
+                }
                 float w[3][W];
-                record_weights<DIM, K>(P, D.hrec[v], c, w);
+                record_weights<DIM, K>(P, R, c, w);
                 float vy[NZ];
 #pragma unroll
                 for (int j2 = 0; j2 < NZ; ++j2)
@@ -282,7 +294,7 @@ units_item(const DevPlan& D, int item, int* s_order, int* s_start)
                     const float vz = ZS == 1 ? vy[z % NZ] : __shfl_sync(gmask, vy[z % NZ], lead + z / NZ);
                     V = fmaf(DIM == 3 ? w[2][z] : 1.f, vz, V);
                 }
-                if (zh == 0) Qi[(long long)P.Q_depth * (D.home_list[v] - P.marker0) + c] = V;
+                if (zh == 0) Qi[(long long)P.Q_depth * (g - P.marker0) + c] = V;
             }
         }
     }
