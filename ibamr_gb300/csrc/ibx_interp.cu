@@ -48,10 +48,18 @@ __global__ void __launch_bounds__(INTERP_THREADS, 3) interp_chunks_sparse(const 
     chunk_body<DIM, K, false>(D, blockIdx.x * (long long)blockDim.x + threadIdx.x, SEL_SPARSE, 0);
 }
 
+// CTAs per SM the per-unit interpolation's registers are cut for: 3 in 3D
+// (80 registers; at 64 its cached planes spill), 4 in 2D (64, no spill).
+template <int DIM>
+struct UnitsOccupancy
+{
+    static constexpr int value = DIM == 3 ? 3 : 4;
+};
+
 // Dense-homed markers by home unit (units_item); items are taken from a
 // counter (no tail from CTAs resident late).
 template <int DIM, int K>
-__global__ void __launch_bounds__(INTERP_THREADS) interp_units(const DevPlan D)
+__global__ void __launch_bounds__(INTERP_THREADS, UnitsOccupancy<DIM>::value) interp_units(const DevPlan D)
 {
     const int n_items = min(D.items[D.n_tiles], D.n_item_cap);
     __shared__ int s_item;
