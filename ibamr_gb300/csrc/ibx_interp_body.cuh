@@ -113,12 +113,20 @@ chunk_body(const DevPlan& D, long long tid, int select, int marker_order)
     float u[CACHE ? NF : 1];
     int cur[3] = { -100000, -100000, -100000 };
     int curp = -1;
+    int lastp = 0; // the previous marker's problem: consecutive markers mostly share it
     for (long long m = m0; m < m1; ++m)
     {
         const int g = marker_order ? (int)m : D.home_list[m];
         if (marker_order && D.home_tile[g] < 0) continue;
         if (select != SEL_ALL && tile_dense(D, D.home_tile[g]) != (select == SEL_DENSE)) continue;
-        const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.marker_offs, D.n_probs, (long long)g);
+        int p = 0;
+        if (D.n_probs > 1)
+        {
+            p = (g >= D.marker_offs[lastp] && g < D.marker_offs[lastp + 1])
+                    ? lastp
+                    : find_in_offsets(D.marker_offs, D.n_probs, (long long)g);
+            lastp = p;
+        }
         const PlanProb& P = D.probs[p];
         if (c >= P.ncomp) continue;
         const Rec R = marker_order ? D.rec[g] : D.hrec[m];
