@@ -63,6 +63,13 @@ def lib():
         L.ibx_spring_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.ibx_beam_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int] + \
+            [ctypes.c_void_p] * 6 + [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.ibx_target_point_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_int] + [ctypes.c_void_p] * 5 + \
+            [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.ibx_body_forces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.ibx_cache_local_indices.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
@@ -357,6 +364,58 @@ def spring_forces(dim, X, master, slave, stiffness, rest_length, F, accumulate=F
     if rc:
         raise IbxError(rc, "ibx_spring_forces")
     return status
+
+
+def beam_forces(dim, X, master, next_, prev, rigidity, curvature, F, accumulate=False, status=None, stream=None):
+    """Beam (bending) forces into F (ibx_beam_forces).  Device tensors: X and
+    curvature (dim per beam) float64, master/next_/prev int32, rigidity
+    float64, F float64 or float32.  Returns the status tensor."""
+    import torch
+
+    if status is None:
+        status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    precision = FP64 if F.dtype == torch.float64 else MIXED
+    rc = lib().ibx_beam_forces(int(dim), int(F.numel() // dim), _ptr(X), int(master.numel()), _ptr(master),
+                               _ptr(next_), _ptr(prev), _ptr(rigidity), _ptr(curvature), _ptr(F), precision,
+                               1 if accumulate else 0, _ptr(status), _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_beam_forces")
+    return status
+
+
+def target_point_forces(dim, X, U, node, kappa, eta, X_target, F, accumulate=False, max_displacement=None,
+                        status=None, stream=None):
+    """Target-point forces into F (ibx_target_point_forces).  U may be None
+    (zero velocities); max_displacement, a one-element float64 device tensor
+    or None, receives the largest |X_target - X|.  Returns the status
+    tensor."""
+    import torch
+
+    if status is None:
+        status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    precision = FP64 if F.dtype == torch.float64 else MIXED
+    rc = lib().ibx_target_point_forces(int(dim), int(F.numel() // dim), _ptr(X), _ptr(U) if U is not None else None,
+                                       int(node.numel()), _ptr(node), _ptr(kappa), _ptr(eta), _ptr(X_target),
+                                       _ptr(F), precision, 1 if accumulate else 0,
+                                       _ptr(max_displacement) if max_displacement is not None else None,
+                                       _ptr(status), _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_target_point_forces")
+    return status
+
+
+def body_forces(dim, structure, force, F, has_force=None, stream=None):
+    """Uniform body forces of structures added into F (ibx_body_forces):
+    structure int32 per marker, force float64 (dim per structure id),
+    has_force int32 per structure id or None (every structure)."""
+    import torch
+
+    precision = FP64 if F.dtype == torch.float64 else MIXED
+    rc = lib().ibx_body_forces(int(dim), int(F.numel() // dim), _ptr(structure), int(force.numel() // dim),
+                               _ptr(force), _ptr(has_force) if has_force is not None else None, _ptr(F), precision,
+                               _stream_handle(stream))
+    if rc:
+        raise IbxError(rc, "ibx_body_forces")
 
 
 def accumulate_ghosts(problem, periodic, stream=None):

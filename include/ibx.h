@@ -272,6 +272,32 @@ int ibx_fe_assemble_rhs(const ibx_fe_mesh* mesh, const ibx_quad_rule* rule, cons
 int ibx_spring_forces(int dim, int n_markers, const double* X, int n_springs, const int* master, const int* slave,
                       const double* stiffness, const double* rest_length, void* F, int precision, int accumulate,
                       int* status, void* stream);
+/* IBStandardForceGen::computeLagrangianBeamForce
+ * (src/IB/IBStandardForceGen.cpp:1037-1147) on the device: for beam k with
+ * master node master[k] and neighbours next[k], prev[k], rigidity K =
+ * rigidity[k] and reference curvature D2X0 = curvature[dim*k ..],
+ * F = K * ((X_next + X_prev) - 2 X_master - D2X0); 2F is added to the master
+ * node's force, F subtracted from each neighbour's.  Arguments, precision,
+ * accumulate and status as for ibx_spring_forces. */
+int ibx_beam_forces(int dim, int n_markers, const double* X, int n_beams, const int* master, const int* next,
+                    const int* prev, const double* rigidity, const double* curvature, void* F, int precision,
+                    int accumulate, int* status, void* stream);
+/* IBStandardForceGen::computeLagrangianTargetPointForce (:1201-1299) on the
+ * device: for target point k at node node[k], F += kappa[k] *
+ * (X_target[dim*k ..] - X) - eta[k] * U (U: the nodes' velocities, dim per
+ * marker; NULL = 0).  max_displacement (a device double, or NULL) receives
+ * the largest |X_target - X| over the points, the value the reference logs.
+ * Arguments, precision, accumulate and status as for ibx_spring_forces. */
+int ibx_target_point_forces(int dim, int n_markers, const double* X, const double* U, int n_points, const int* node,
+                            const double* kappa, const double* eta, const double* X_target, void* F, int precision,
+                            int accumulate, double* max_displacement, int* status, void* stream);
+/* IBStandardForceGen::computeLagrangianBodyForce (:1301-1327) on the device:
+ * marker i of structure structure[i] gets the structure's uniform force
+ * force[dim*sid ..] added to F, for sid in [0, n_structures) with
+ * has_force[sid] != 0 (has_force NULL: every structure).  Device pointers;
+ * F as for ibx_spring_forces (always accumulated). */
+int ibx_body_forces(int dim, int n_markers, const int* structure, int n_structures, const double* force,
+                    const int* has_force, void* F, int precision, void* stream);
 
 /* ---- host helpers (used by the C++ LEInteractor layer) ----------------- */
 /* Device memory and copies for callers without the CUDA runtime headers.

@@ -72,6 +72,26 @@ def test_plan_knobs_reject_a_null_plan(libibx):
     assert L.ibx_plan_step_io(None, None, 0, None, 0, None, 0, None) == E_ARG
 
 
+def test_force_entry_points_validate_on_the_host(libibx):
+    """Argument errors of the Lagrangian force entry points are found before
+    any device call: a bad dimension, a missing status word, missing arrays;
+    empty inputs succeed without a launch."""
+    L = ctypes.CDLL(libibx)
+    E_ARG = 4
+    vp = ctypes.c_void_p
+    L.ibx_beam_forces.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int] + [vp] * 6 + [ctypes.c_int,
+                                                                                             ctypes.c_int, vp, vp]
+    assert L.ibx_beam_forces(4, 0, None, 0, None, None, None, None, None, None, 0, 1, None, None) == E_ARG
+    assert L.ibx_beam_forces(2, 0, None, 0, None, None, None, None, None, None, 0, 1, None, None) == E_ARG
+    L.ibx_target_point_forces.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int] + [vp] * 5 + [
+        ctypes.c_int, ctypes.c_int, vp, vp, vp]
+    assert L.ibx_target_point_forces(2, 0, None, None, 3, None, None, None, None, None, 0, 1, None, None,
+                                     None) == E_ARG
+    L.ibx_body_forces.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, vp]
+    assert L.ibx_body_forces(3, 0, None, 0, None, None, None, 0, None) == 0
+    assert L.ibx_body_forces(3, 10, None, 2, None, None, None, 0, None) == E_ARG
+
+
 def test_host_queries(libibx):
     L = ctypes.CDLL(libibx)
     L.ibx_status_string.restype = ctypes.c_char_p
