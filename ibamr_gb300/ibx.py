@@ -285,11 +285,19 @@ def cache_local_indices(dim, ilower, iupper, x_lower, x_upper, dx, touches_perio
     return idx[:m], sh[: m * dim], cells[: m * dim]
 
 
+FE_SIMPLEX_P1, FE_TENSOR_Q1 = 0, 1
+
+
 class FeMesh(ctypes.Structure):
-    """ibx_fe_mesh: first-order simplex mesh (device arrays)."""
+    """ibx_fe_mesh: first-order Lagrange mesh of one element family (device
+    arrays)."""
 
     _fields_ = [("dim", ctypes.c_int), ("n_nodes", ctypes.c_int), ("n_elems", ctypes.c_int),
-                ("elem_nodes", ctypes.c_void_p), ("X", ctypes.c_void_p)]
+                ("elem_nodes", ctypes.c_void_p), ("X", ctypes.c_void_p), ("elem_type", ctypes.c_int)]
+
+
+def fe_nodes_per_elem(dim, elem_type):
+    return (4 if dim == 2 else 8) if elem_type == FE_TENSOR_Q1 else dim + 1
 
 
 class QuadRule(ctypes.Structure):
@@ -298,13 +306,14 @@ class QuadRule(ctypes.Structure):
     _fields_ = [("n_points", ctypes.c_int), ("points", ctypes.c_void_p), ("weights", ctypes.c_void_p)]
 
 
-def _fe_args(dim, elem_nodes, X, points, weights):
+def _fe_args(dim, elem_nodes, X, points, weights, elem_type=FE_SIMPLEX_P1):
     import numpy as np
 
     M = FeMesh()
     M.dim = dim
+    M.elem_type = elem_type
     M.n_nodes = X.numel() // dim
-    M.n_elems = elem_nodes.numel() // (dim + 1)
+    M.n_elems = elem_nodes.numel() // fe_nodes_per_elem(dim, elem_type)
     M.elem_nodes = _ptr(elem_nodes).value
     M.X = _ptr(X).value
     pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
@@ -316,12 +325,13 @@ def _fe_args(dim, elem_nodes, X, points, weights):
     return M, R, (pts, w)
 
 
-def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0, stream=None):
+def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0, elem_type=FE_SIMPLEX_P1,
+                         stream=None):
     """FEDataManager::spread's quadrature points (ibx_fe_quadrature_points):
     returns (X_qp, F_JxW_qp or None, JxW) float64 device tensors."""
     import torch
 
-    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights)
+    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights, elem_type)
     nq = M.n_elems * R.n_points
     X_qp = torch.empty(max(nq, 1) * dim, dtype=torch.float64, device=X.device)
     JxW = torch.empty(max(nq, 1), dtype=torch.float64, device=X.device)
@@ -337,10 +347,10 @@ def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0, 
     return X_qp[: nq * dim], None if F_qp is None else F_qp[: nq * n_vars], JxW[:nq]
 
 
-def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars, rhs, stream=None):
+def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars, rhs, elem_type=FE_SIMPLEX_P1, stream=None):
     """FEDataManager::interp's right-hand side (ibx_fe_assemble_rhs): adds into
     rhs (float64 device tensor, n_vars per node)."""
-    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights)
+    M, R, keep = _fe_args(dim, elem_nodes, X, points, weights, elem_type)
     rc = lib().ibx_fe_assemble_rhs(ctypes.byref(M), ctypes.byref(R), _ptr(U_qp), int(n_vars), _ptr(rhs),
                                    _stream_handle(stream))
     del keep

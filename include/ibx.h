@@ -206,10 +206,19 @@ int ibx_cache_local_indices(const ibx_patch_geometry* patch, const int* periodic
                             double* periodic_shifts, int* cells, int* count, void* stream);
 
 /* ---- finite-element quadrature points (FEDataManager) ------------------- */
-/* A mesh of first-order Lagrange simplices (TRI3 in 2D, TET4 in 3D): node k
- * of element e is elem_nodes[(dim+1)*e + k] (libMesh's vertex order: the
- * reference element's vertices 0, e_1, ..., e_dim); X holds dim coordinates
- * per node.  Both are device arrays. */
+/* Element families of ibx_fe_mesh (first-order Lagrange elements). */
+enum
+{
+    IBX_FE_SIMPLEX_P1 = 0, /* TRI3 (2D), TET4 (3D) */
+    IBX_FE_TENSOR_Q1 = 1   /* QUAD4 (2D), HEX8 (3D) */
+};
+/* A mesh of one element family.  Simplices: node k of element e is
+ * elem_nodes[(dim+1)*e + k] (libMesh's vertex order: the reference element's
+ * vertices 0, e_1, ..., e_dim).  Tensor-product cells: node k of element e is
+ * elem_nodes[npe*e + k], npe = 4 (QUAD4) or 8 (HEX8), in libMesh's order on
+ * the reference cell [-1, 1]^dim: (-1,-1), (1,-1), (1,1), (-1,1) in each z
+ * layer, the z = -1 layer first.  X holds dim coordinates per node.  Both
+ * are device arrays.  elem_type: IBX_FE_SIMPLEX_P1 or IBX_FE_TENSOR_Q1. */
 typedef struct ibx_fe_mesh
 {
     int dim;
@@ -217,12 +226,13 @@ typedef struct ibx_fe_mesh
     int n_elems;
     const int* elem_nodes;
     const double* X;
+    int elem_type;
 } ibx_fe_mesh;
 
-/* A quadrature rule on the reference simplex (host arrays): n_points points
- * (dim reference coordinates each) and their weights (summing to the
- * reference element's measure, 1/2 in 2D and 1/6 in 3D, as libMesh's
- * rules do); at most 64 points. */
+/* A quadrature rule on the reference element (host arrays): n_points points
+ * (dim reference coordinates each) and their weights, summing to the
+ * reference element's measure as libMesh's rules do (simplices: 1/2 in 2D,
+ * 1/6 in 3D; tensor-product cells: 4 in 2D, 8 in 3D); at most 64 points. */
 typedef struct ibx_quad_rule
 {
     int n_points;
@@ -234,8 +244,10 @@ typedef struct ibx_quad_rule
  * (ibtk/src/lagrangian/FEDataManager.cpp:1088-1219, sum_weighted_elem_solution
  * :824-858): for point q of element e (entry e*n_points + q),
  * X_qp = sum_k X_k phi_k(q) and, when F_nodes is given (n_vars values per
- * node), F_JxW_qp = (sum_k F_k phi_k(q)) * JxW(q), with the barycentric basis
- * phi and JxW(q) = |det J| * weight(q); JxW receives JxW(q) when not NULL.
+ * node), F_JxW_qp = (sum_k F_k phi_k(q)) * JxW(q), with the element's basis
+ * phi (barycentric on simplices; products of the 1D linear shapes
+ * (1 -+ xi)/2 on tensor-product cells) and JxW(q) = |det J(q)| * weight(q),
+ * J(q) = sum_k X_k (grad phi_k(q))^T; JxW receives JxW(q) when not NULL.
  * Sums run from zero over the basis in order, every operation rounded as
  * written.  The outputs feed ibx_spread (positions X_qp, values F_JxW_qp) as
  * LEInteractor::spread's raw-array form does in the reference.  An element

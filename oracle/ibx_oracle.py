@@ -336,8 +336,71 @@ class CpuPlan:
 
 
 # ---------------------------------------------------------------------------
-# Finite-element quadrature points (FEDataManager, first-order simplices).
+# Finite-element quadrature points (FEDataManager, first-order Lagrange
+# simplices TRI3 / TET4 and tensor-product cells QUAD4 / HEX8).
 # ---------------------------------------------------------------------------
+FE_SIMPLEX_P1, FE_TENSOR_Q1 = 0, 1
+
+# Reference-cell corner of each QUAD4 / HEX8 node in libMesh's order (0: -1,
+# 1: +1 along each axis): counter-clockwise per z layer, z = -1 first.
+_Q1_CORNER = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+
+def _fe_npe(dim, elem_type):
+    return (4 if dim == 2 else 8) if elem_type == FE_TENSOR_Q1 else dim + 1
+
+
+def _fe_q1_basis(dim, points):
+    """QUAD4 / HEX8 basis at the reference points: phi_k = prod_c L(xi_c)
+    with L = (1 - xi) / 2 or (1 + xi) / 2 by the node's corner, the product in
+    axis order; dphi_k / dxi_c the same product with the derivative +-1/2 on
+    axis c.  Returns (phi [n_qp, npe], dphi [n_qp, npe, dim])."""
+    P = np.asarray(points, dtype=np.float64).reshape(-1, dim)
+    npe = 4 if dim == 2 else 8
+    phi = np.zeros((P.shape[0], npe))
+    dphi = np.zeros((P.shape[0], npe, dim))
+    for k in range(npe):
+        L = [np.where(_Q1_CORNER[k, c], 0.5 * (1.0 + P[:, c]), 0.5 * (1.0 - P[:, c])) for c in range(dim)]
+        dL = [np.full(P.shape[0], 0.5 if _Q1_CORNER[k, c] else -0.5) for c in range(dim)]
+        p = L[0]
+        for c in range(1, dim):
+            p = p * L[c]
+        phi[:, k] = p
+        for c in range(dim):
+            g = dL[0] if c == 0 else L[0]
+            for a in range(1, dim):
+                g = g * (dL[a] if a == c else L[a])
+            dphi[:, k, c] = g
+    return phi, dphi
+
+
+def _det(dim, J):
+    """det of J[..., r, c], the products and differences in a fixed order."""
+    if dim == 2:
+        return J[..., 0, 0] * J[..., 1, 1] - J[..., 0, 1] * J[..., 1, 0]
+    m0 = J[..., 1, 1] * J[..., 2, 2] - J[..., 1, 2] * J[..., 2, 1]
+    m1 = J[..., 1, 0] * J[..., 2, 2] - J[..., 1, 2] * J[..., 2, 0]
+    m2 = J[..., 1, 0] * J[..., 2, 1] - J[..., 1, 1] * J[..., 2, 0]
+    return (J[..., 0, 0] * m0 - J[..., 0, 1] * m1) + J[..., 0, 2] * m2
+
+
+def _fe_q1_jxw(dim, elem_nodes, X, points, weights):
+    """JxW [n_elems, n_qp] of a QUAD4 / HEX8 mesh: |det J(q)| w(q) with
+    J(q)_rc = sum_k X_k[r] dphi_k/dxi_c (q), summed from zero in node order."""
+    npe = 4 if dim == 2 else 8
+    E = np.asarray(elem_nodes).reshape(-1, npe)
+    Xn = np.asarray(X, dtype=np.float64).reshape(-1, dim)
+    _, dphi = _fe_q1_basis(dim, points)
+    nq = dphi.shape[0]
+    J = np.zeros((E.shape[0], nq, dim, dim))
+    for r in range(dim):
+        for c in range(dim):
+            v = np.zeros((E.shape[0], nq))
+            for k in range(npe):
+                v = v + Xn[E[:, k], r][:, None] * dphi[None, :, k, c]
+            J[:, :, r, c] = v
+    w = np.asarray(weights, dtype=np.float64).reshape(-1)
+    return np.abs(_det(dim, J)) * w[None, :]
 
 def _fe_phi(dim, points):
     """Barycentric basis at the reference points: phi_0 = 1 - (xi_0 + ... ),
@@ -363,50 +426,61 @@ def _fe_abs_det(dim, elem_nodes, X):
     return np.abs(det)
 
 
-def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0):
+def fe_quadrature_points(dim, elem_nodes, X, points, weights, F=None, n_vars=0, elem_type=FE_SIMPLEX_P1):
     """FEDataManager::spread's quadrature-point values
     (ibtk/src/lagrangian/FEDataManager.cpp:1088-1219 with
     sum_weighted_elem_solution :824-858): X_q = sum_k X_k phi_k(q) and
     F_q = (sum_k F_k phi_k(q)) * JxW(q), the sums from zero over the basis in
-    order, JxW(q) = |det J| * w(q).  Returns (X_qp, F_qp or None, JxW),
+    order, JxW(q) = |det J(q)| * w(q).  Returns (X_qp, F_qp or None, JxW),
     entries e * n_qp + q."""
-    E = np.asarray(elem_nodes).reshape(-1, dim + 1)
+    npe = _fe_npe(dim, elem_type)
+    E = np.asarray(elem_nodes).reshape(-1, npe)
     Xn = np.asarray(X, dtype=np.float64).reshape(-1, dim)
-    phi = _fe_phi(dim, points)
     w = np.asarray(weights, dtype=np.float64).reshape(-1)
+    if elem_type == FE_TENSOR_Q1:
+        phi, _ = _fe_q1_basis(dim, points)
+        jxw = _fe_q1_jxw(dim, elem_nodes, X, points, weights)
+    else:
+        phi = _fe_phi(dim, points)
+        jxw = _fe_abs_det(dim, elem_nodes, X)[:, None] * w[None, :]
     nq = w.size
     ne = E.shape[0]
     X_qp = np.zeros((ne, nq, dim))
-    for k in range(dim + 1):
+    for k in range(npe):
         X_qp = X_qp + Xn[E[:, k]][:, None, :] * phi[None, :, k, None]
-    jxw = _fe_abs_det(dim, elem_nodes, X)[:, None] * w[None, :]
     F_qp = None
     if F is not None:
         Fn = np.asarray(F, dtype=np.float64).reshape(-1, n_vars)
         acc = np.zeros((ne, nq, n_vars))
-        for k in range(dim + 1):
+        for k in range(npe):
             acc = acc + Fn[E[:, k]][:, None, :] * phi[None, :, k, None]
         F_qp = (acc * jxw[:, :, None]).reshape(-1)
     return X_qp.reshape(-1), F_qp, jxw.reshape(-1)
 
 
-def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars):
+def fe_assemble_rhs(dim, elem_nodes, X, points, weights, U_qp, n_vars, elem_type=FE_SIMPLEX_P1):
     """FEDataManager::interp's right-hand side (FEDataManager.cpp:1873-2005,
     integrate_elem_rhs :1569-1604): rhs[node_k] += sum_q U_q * (phi_k(q) *
     JxW(q)) per element, the element sums in point order, the elements added
     in order.  Returns rhs [n_nodes * n_vars]."""
-    E = np.asarray(elem_nodes).reshape(-1, dim + 1)
+    npe = _fe_npe(dim, elem_type)
+    E = np.asarray(elem_nodes).reshape(-1, npe)
     n_nodes = np.asarray(X).size // dim
-    phi = _fe_phi(dim, points)
     w = np.asarray(weights, dtype=np.float64).reshape(-1)
     nq = w.size
-    det = _fe_abs_det(dim, elem_nodes, X)
+    if elem_type == FE_TENSOR_Q1:
+        phi, _ = _fe_q1_basis(dim, points)
+        jxw = _fe_q1_jxw(dim, elem_nodes, X, points, weights)
+    else:
+        phi = _fe_phi(dim, points)
+        det = _fe_abs_det(dim, elem_nodes, X)
+        jxw = np.stack([det * w[q] for q in range(nq)], axis=1)
     U = np.asarray(U_qp, dtype=np.float64).reshape(E.shape[0], nq, n_vars)
     rhs = np.zeros((n_nodes, n_vars))
-    for k in range(dim + 1):
+    for k in range(npe):
         acc = np.zeros((E.shape[0], n_vars))
         for q in range(nq):
-            p_jxw = phi[q, k] * (det * w[q])
+            p_jxw = phi[q, k] * jxw[:, q]
             acc = acc + U[:, q, :] * p_jxw[:, None]
         np.add.at(rhs, E[:, k], acc)
     return rhs.reshape(-1)

@@ -1,9 +1,10 @@
 """The finite-element quadrature-point path (FEDataManager::spread / interp,
 ibtk/src/lagrangian/FEDataManager.cpp:1088-1219, 1873-2005) for first-order
-simplex meshes, on the device: quadrature-point positions, F * JxW and JxW
-bit-identical to the oracle's restatement; the spread of those values (the
-raw-array LEInteractor::spread) and the interpolation at the quadrature
-points followed by the right-hand-side assembly within 1e-12 of the oracle."""
+Lagrange meshes (TRI3 / TET4 simplices and QUAD4 / HEX8 cells), on the
+device: quadrature-point positions, F * JxW and JxW bit-identical to the
+oracle's restatement; the spread of those values (the raw-array
+LEInteractor::spread) and the interpolation at the quadrature points followed
+by the right-hand-side assembly within 1e-12 of the oracle."""
 
 import numpy as np
 import pytest
@@ -142,3 +143,77 @@ def test_fe_rhs_of_a_constant_field(ibx):
 
     vol = float(np.sum(ibx_oracle._fe_abs_det(3, E, X))) / 6.0
     assert abs(r[:, 0].sum() - vol) <= 1e-12 * vol and abs(r[:, 1].sum() - vol) <= 1e-12 * vol
+
+
+def q1_mesh(dim, m, rng, lo=0.3, hi=0.7):
+    """Perturbed structured QUAD4 (2D) / HEX8 (3D) mesh of [lo, hi]^dim in
+    libMesh's node order (counter-clockwise per z layer, z = lo first)."""
+    g = np.linspace(lo, hi, m + 1)
+    idx = np.stack(np.meshgrid(*([np.arange(m + 1)] * dim), indexing="ij"), axis=-1).reshape(-1, dim)
+    X = g[idx] + rng.uniform(-0.25, 0.25, size=idx.shape) * ((hi - lo) / m)
+    stride = [(m + 1) ** (dim - 1 - d) for d in range(dim)]
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)][: 2 ** dim]
+    E = []
+    for cell in np.ndindex(*([m] * dim)):
+        E += [sum((cell[d] + c[d]) * stride[d] for d in range(dim)) for c in corners]
+    return np.array(E, dtype=np.int32), X.reshape(-1)
+
+
+def gauss_rule(dim, n):
+    """Tensor-product Gauss rule with n points per axis on [-1, 1]^dim."""
+    x, w = np.polynomial.legendre.leggauss(n)
+    P = np.stack(np.meshgrid(*([x] * dim), indexing="ij"), -1).reshape(-1, dim)
+    W = np.prod(np.stack(np.meshgrid(*([w] * dim), indexing="ij"), -1).reshape(-1, dim), axis=1)
+    return P, W
+
+
+@pytest.mark.parametrize("n_gauss", [2, 3])
+@pytest.mark.parametrize("dim,m", [(2, 20), (3, 6)])
+def test_q1_quadrature_points_bit_identical(ibx, oracle, dim, m, n_gauss):
+    """QUAD4 / HEX8 cells: positions, F * JxW and JxW (the Jacobian taken at
+    every point) bit-identical to the oracle's restatement."""
+    rng = np.random.default_rng(60 + dim + n_gauss)
+    E, X = q1_mesh(dim, m, rng)
+    pts, w = gauss_rule(dim, n_gauss)
+    F = rng.standard_normal(X.size)
+    Xq_ref, Fq_ref, J_ref = oracle.fe_quadrature_points(dim, E, X, pts, w, F=F, n_vars=dim,
+                                                        elem_type=oracle.FE_TENSOR_Q1)
+    Xq, Fq, J = ibx.fe_quadrature_points(dim, torch.tensor(E, device="cuda"), torch.tensor(X, device="cuda"), pts,
+                                         w, F=torch.tensor(F, device="cuda"), n_vars=dim,
+                                         elem_type=ibx.FE_TENSOR_Q1)
+    assert np.array_equal(Xq.cpu().numpy(), Xq_ref)
+    assert np.array_equal(J.cpu().numpy(), J_ref)
+    assert np.array_equal(Fq.cpu().numpy(), Fq_ref)
+
+
+@pytest.mark.parametrize("dim,m,N", [(2, 20, 64), (3, 6, 32)])
+def test_q1_spread_and_interp_against_oracle(ibx, oracle, dim, m, N):
+    """A QUAD4 / HEX8 structure through FEDataManager's path: spread of
+    F * JxW from the quadrature points, interpolation there and the
+    projection's right-hand side, against the oracle (FP64 within 1e-12)."""
+    rng = np.random.default_rng(70 + dim)
+    E, X = q1_mesh(dim, m, rng)
+    pts, w = gauss_rule(dim, 2)
+    F = rng.standard_normal(X.size)
+    Q1 = oracle.FE_TENSOR_Q1
+    Xq_ref, Fq_ref, _ = oracle.fe_quadrature_points(dim, E, X, pts, w, F=F, n_vars=dim, elem_type=Q1)
+    u = rng.standard_normal([dim] + [N] * dim)
+    f_ref, U_ref = oracle.periodic_problem(dim, [N] * dim, "IB_4", Xq_ref, F=Fq_ref, u=u, centering=1)
+    rhs_ref = oracle.fe_assemble_rhs(dim, E, X, pts, w, U_ref, dim, elem_type=Q1)
+    E_t, X_t = torch.tensor(E, device="cuda"), torch.tensor(X, device="cuda")
+    Xq, Fq, _ = ibx.fe_quadrature_points(dim, E_t, X_t, pts, w, F=torch.tensor(F, device="cuda"), n_vars=dim,
+                                         elem_type=ibx.FE_TENSOR_Q1)
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [N - 1] * dim,
+                                       [1.0 / N] * dim, [0.0] * dim, [1.0] * dim, q, Xq, Q)
+    f = [torch.zeros([N] * dim, dtype=torch.float64, device="cuda") for _ in range(dim)]
+    ibx.spread(mk(f, Fq), "IB_4", ibx.FP64)
+    u_t = [torch.tensor(u[a], device="cuda") for a in range(dim)]
+    Uq = torch.zeros(Xq.numel(), dtype=torch.float64, device="cuda")
+    ibx.interpolate(mk(u_t, Uq), "IB_4", ibx.FP64)
+    rhs = torch.zeros(X.size, dtype=torch.float64, device="cuda")
+    ibx.fe_assemble_rhs(dim, E_t, X_t, pts, w, Uq, dim, rhs, elem_type=ibx.FE_TENSOR_Q1)
+    torch.cuda.synchronize()
+    fs = np.stack([t.cpu().numpy() for t in f])
+    assert np.max(np.abs(fs - f_ref)) <= 1e-12 * np.max(np.abs(f_ref))
+    assert np.max(np.abs(Uq.cpu().numpy() - U_ref)) <= 1e-12 * np.max(np.abs(U_ref))
+    assert np.max(np.abs(rhs.cpu().numpy() - rhs_ref)) <= 1e-12 * np.max(np.abs(rhs_ref))
