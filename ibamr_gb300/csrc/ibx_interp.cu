@@ -11,9 +11,10 @@
 //    ones (form 1), or every marker in the caller's order (form 2: it needs
 //    only the stencil records, so the step can start it before the counting
 //    sort; fibre markers given in fibre order share runs as in home order).
-//    In form 1 the sparse-homed markers, which seldom share a stencil, go
-//    to interp_chunks_sparse: the same sums without the register cache, in
-//    80 registers instead of 128 (24 resident warps per SM instead of 16).
+//    In forms 1 and 4 the sparse-homed markers, which seldom share a
+//    stencil, go to interp_chunks_sparse: the same sums without the register
+//    cache, in 80 registers instead of 128 (24 resident warps per SM instead
+//    of 16).
 //  - interp_units (form 1, dense-homed): the work items of the dense spread
 //    (item_units home units of one tile); a group of lanes per (unit,
 //    component), the footprint's z-planes split over the group, loads the
@@ -378,7 +379,7 @@ launch_interp_k(const DevPlan& D, cudaStream_t s)
         const long long chunks = (D.n_markers + CHUNK - 1) / CHUNK;
         const unsigned bx = (unsigned)((chunks * D.max_ncomp + INTERP_THREADS - 1) / INTERP_THREADS);
         if (bx == 0) return IBX_OK;
-        interp_chunks<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D, SEL_SPARSE, 0);
+        interp_chunks_sparse<DIM, K><<<bx, INTERP_THREADS, 0, s>>>(D);
         note_launches(1);
         return cudaGetLastError() == cudaSuccess ? IBX_OK : IBX_E_CUDA;
     }

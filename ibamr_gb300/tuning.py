@@ -67,12 +67,13 @@ def _time(fn, reps, stream):
 def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     """Measure candidate settings of ``plan`` and keep the fastest.
 
-    The search runs in three stages, each at the best setting so far: the
-    split between the two spread kernels (``dense_min``) jointly with the
+    The search runs in stages, each at the best setting so far: the split
+    between the two spread kernels (``dense_min``) jointly with the
     per-visit kernel form; the dense-kernel knobs (``item_units``,
-    ``dense_blocks_per_sm``, ``unit_cap``); for plans with their own interpolation targets,
-    the interpolation form jointly with the step mode (concurrent or serial
-    spread and interpolation).  Returns {"best": (item_units, dense_min,
+    ``dense_blocks_per_sm``, ``unit_cap``); for plans with their own
+    interpolation targets, the interpolation form jointly with the step mode
+    (concurrent, serial or fused spread and interpolation), and, when that
+    changed them, the dense-kernel knobs once more.  Returns {"best": (item_units, dense_min,
     dense_blocks_per_sm), "visit_kernel": form, "interp_kernel": form or
     None, "step_mode": mode or None, "unit_cap": cap, "ms": t, "table":
     [((item_units, dense_min, dense_blocks_per_sm, visit_kernel,
@@ -130,6 +131,14 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
         iu, dm, bps, vk, _, _, cap = best_cfg()[0]
         for ik, sm in itertools.product(cand["interp_kernel"], cand["step_mode"]):
             measure((iu, dm, bps, vk, ik, sm, cap))
+        # the dense knobs again under the chosen interpolation form and step
+        # mode: beside a concurrent interpolation fewer dense CTAs can be
+        # best, one after the other more
+        _, dm, _, vk, ik, sm, _ = best_cfg()[0]
+        if (ik, sm) != (ik0, sm0):
+            for iu, bps, cap in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"],
+                                                  cand["unit_cap"]):
+                measure((iu, dm, bps, vk, ik, sm, cap))
     cfg, ms = best_cfg()
     apply(cfg)
     out = {"best": tuple(plan.tuning()), "ms": ms, "table": table, "config": cfg, "visit_kernel": cfg[3],
