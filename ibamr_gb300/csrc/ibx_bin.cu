@@ -230,7 +230,14 @@ __global__ void __launch_bounds__(256) bin_kernel(const DevPlan D)
                 R.rc[d] = R.rs[d] = 0.f;
                 continue;
             }
-            const double X = P.X[DIM * s + d];
+            double X;
+            if (D.x_src)
+            {
+                X = D.x_src[DIM * g + d];
+                D.x_dst[DIM * g + d] = X;
+            }
+            else
+                X = P.X[DIM * s + d];
             finite = finite && isfinite(X);
             const FixedDim& fx = P.fx[d];
             int bc, bs;
@@ -569,13 +576,15 @@ launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 }
 
 int
-bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s, cudaEvent_t records_done)
+bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s, cudaEvent_t records_done,
+             cudaEvent_t records_done2)
 {
     const int nt = D.n_tiles;
     // Counters, cursors and item counts are contiguous: one memset.
     if (cudaMemsetAsync(D.hcount, 0, sizeof(int) * counter_ints(nt), s) != cudaSuccess) return IBX_E_CUDA;
     int rc = launch_bin(dim, kernel, D, s, 0);
     if (!rc && records_done && cudaEventRecord(records_done, s) != cudaSuccess) rc = IBX_E_CUDA;
+    if (!rc && records_done2 && cudaEventRecord(records_done2, s) != cudaSuccess) rc = IBX_E_CUDA;
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
     if (!rc) rc = launch_bin(dim, kernel, D, s, 1);                 // also counts the work items
     if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 2, scan_tmp, s); // vcount, items

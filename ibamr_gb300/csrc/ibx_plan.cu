@@ -163,6 +163,10 @@ struct ibx_plan
     // for it (ev_q)
     cudaStream_t up;
     cudaEvent_t ev_x, ev_q;
+    // The problems' positions as one array in global marker order (problem
+    // p's X at base + dim * its first marker), or null: then positions copied
+    // into it from page-locked host memory are read by the binning directly.
+    double* x_base;
     int step_mode;
     int n_tma; // problems whose interpolation sources have tensor maps
 };
@@ -296,6 +300,9 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     z.tile_shape = tile_shape;
     z.n_probs = n_problems;
     z.n_markers = moffs[n_problems];
+    bool x_contiguous = true;
+    for (int p = 0; p < n_problems; ++p)
+        x_contiguous = x_contiguous && hp[p].X == hp[0].X + (long long)dim * moffs[p];
     z.n_tiles = toffs[n_problems];
     z.visit_cap = visit_cap;
     z.item_cap = item_cap;
@@ -331,6 +338,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     }
     plan->scan_tmp = c.scan_tmp;
     plan->step_mode = 1;
+    plan->x_base = x_contiguous ? const_cast<double*>(hp[0].X) : nullptr;
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
         cudaStreamCreateWithPriority(&plan->side, cudaStreamNonBlocking, least) != cudaSuccess ||
@@ -396,18 +404,42 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
           const ibx_transfer* out_Q, int n_out_Q)
 {
     using namespace ibx;
-    int rc = copy_all(in_X, n_in_X, s);
+    // Positions that fill the plan's whole position array from page-locked
+    // host memory are read by the binning itself over the host link (and
+    // stored into the array on the way): no separate copy before it.
+    DevPlan D = plan->D;
+    bool direct = false;
+    if (n_in_X == 1 && plan->x_base && in_X[0].dst == plan->x_base &&
+        in_X[0].bytes == sizeof(double) * (size_t)plan->dim * (size_t)plan->D.n_markers)
+    {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, in_X[0].src) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+            a.devicePointer)
+        {
+            direct = true;
+            D.x_src = static_cast<const double*>(a.devicePointer);
+            D.x_dst = plan->x_base;
+        }
+        cudaGetLastError(); // an unregistered pointer leaves an error behind on some runtimes
+    }
+    int rc = direct ? IBX_OK : copy_all(in_X, n_in_X, s);
     if (rc) return rc;
     bool up = false;
     for (int i = 0; i < n_in_Q; ++i) up = up || in_Q[i].bytes > 0;
-    if (up)
-    {
-        if (cudaEventRecord(plan->ev_x, s) != cudaSuccess || cudaStreamWaitEvent(plan->up, plan->ev_x, 0) != cudaSuccess)
-            return IBX_E_CUDA;
-        rc = copy_all(in_Q, n_in_Q, plan->up);
+    // the spread values go up behind the positions: after the copy, or after
+    // the binning kernel that reads the positions directly
+    auto upload = [&]() -> int {
+        if (!up) return IBX_OK;
+        if (cudaStreamWaitEvent(plan->up, plan->ev_x, 0) != cudaSuccess) return IBX_E_CUDA;
+        const int r = copy_all(in_Q, n_in_Q, plan->up);
         if (cudaEventRecord(plan->ev_q, plan->up) != cudaSuccess) return IBX_E_CUDA;
-        if (rc)
-            return cudaStreamWaitEvent(s, plan->ev_q, 0) == cudaSuccess ? rc : IBX_E_CUDA;
+        return r;
+    };
+    if (up && !direct)
+    {
+        if (cudaEventRecord(plan->ev_x, s) != cudaSuccess) return IBX_E_CUDA;
+        rc = upload();
+        if (rc) return cudaStreamWaitEvent(s, plan->ev_q, 0) == cudaSuccess ? rc : IBX_E_CUDA;
     }
     // joins the upload into `st` (the stream the spread runs on)
     auto wait_up = [&](cudaStream_t st) { return !up || cudaStreamWaitEvent(st, plan->ev_q, 0) == cudaSuccess; };
@@ -415,7 +447,18 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     // concurrent mode it forks as soon as they exist, beside the counting
     // sort; the other forms fork after the whole binning.
     const bool early = plan->step_mode == 1 && plan->D.interp_form == 2;
-    rc = bin_sequence(plan->dim, plan->kernel, plan->D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr);
+    rc = bin_sequence(plan->dim, plan->kernel, D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr,
+                      up && direct ? plan->ev_x : nullptr);
+    if (up && direct)
+    {
+        const int ru = rc ? IBX_OK : upload();
+        if (rc || ru)
+        {
+            // the upload stream waited on an event of this step or nothing: join it
+            if (cudaEventRecord(plan->ev_q, plan->up) == cudaSuccess) cudaStreamWaitEvent(s, plan->ev_q, 0);
+            return rc ? rc : ru;
+        }
+    }
     if (rc) return wait_up(s) ? rc : IBX_E_CUDA;
     bool out = false;
     for (int i = 0; i < n_out_Q; ++i) out = out || out_Q[i].bytes > 0;

@@ -160,6 +160,13 @@ struct DevPlan
     // Tensor maps of the interpolation sources, 3 per problem (one per
     // component), valid where the problem's tma flag is set.
     const CUtensorMap* tmaps;
+    // Positions of this step read from page-locked host memory by the
+    // binning (x_src, dim values per marker in global marker order) and
+    // stored on the way into the plan's position array (x_dst); null: the
+    // binning reads the problems' X.  Set only in the copy of the plan passed
+    // to one step's binning (ibx_plan_step_io).
+    const double* x_src;
+    double* x_dst;
 };
 
 // Region of an interpolation source staged for the markers homed in one
@@ -232,10 +239,11 @@ bool fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx);
 
 // The binning sequence of one step (counters zeroed, bin, scans, scatters,
 // dense work items).
-// Binning of a plan on stream s; records_done (optional) is recorded once the
-// stencil records and home tiles exist (before the counting sort).
+// Binning of a plan on stream s; records_done and records_done2 (optional)
+// are recorded once the stencil records and home tiles exist (before the
+// counting sort).
 int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s,
-                 cudaEvent_t records_done = nullptr);
+                 cudaEvent_t records_done = nullptr, cudaEvent_t records_done2 = nullptr);
 
 template <typename T>
 __device__ __forceinline__ int

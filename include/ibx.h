@@ -376,8 +376,12 @@ typedef struct ibx_transfer
 /* ibx_plan_step with the step's host transfers ordered around it, for a
  * caller whose marker data live in host memory (no reference counterpart:
  * the reference's LData are host arrays, which this call moves in and out).
- * in_X (positions) are copied first, on `stream`; in_Q (the values to
- * spread) on a stream of the plan behind them, beside the binning, and the
+ * in_X (positions) are copied first, on `stream` -- or, when in_X is one
+ * copy from page-locked host memory onto the plan's whole position array
+ * (every problem's X one array in marker order), read by the binning kernel
+ * straight from the host buffer and stored into the array on the way;
+ * in_Q (the values to spread) on a stream of the plan behind them, beside
+ * the binning, and the
  * spread waits for them; out_Q (the interpolated values) are copied as soon
  * as the interpolation ends, beside the rest of the spread (with out_Q the
  * concurrent mode gives the interpolation the greater stream priority, so

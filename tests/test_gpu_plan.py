@@ -452,13 +452,17 @@ def test_fused_step_matches_oracle_and_separate_launches(ibx, oracle, kernel, di
     plan.close()
 
 
+@pytest.mark.parametrize("x_source", ["pinned", "device"])
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("step_mode", [0, 1, 2])
 @pytest.mark.parametrize("interp_form", [1, 2])
-def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, interp_form):
+def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, interp_form, x_source):
     """ibx_plan_step_io moves positions and forces in from pinned host memory
-    and the interpolated values out: the oracle's answer eagerly, and from a
-    CUDA graph of the call replayed with new host forces and positions."""
+    (positions read by the binning straight from the host buffer, or copied
+    from a device buffer) and the interpolated values out: the oracle's
+    answer eagerly, and from a CUDA graph of the call replayed with new host
+    forces and positions; the plan's position array holds the positions
+    afterwards either way."""
     rng = np.random.default_rng(151 + dim + 3 * step_mode)
     N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
     n = 2500
@@ -470,7 +474,7 @@ def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, in
     u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
     F_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
     U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
-    Xh = torch.tensor(X).pin_memory()
+    Xh = torch.tensor(X).pin_memory() if x_source == "pinned" else torch.tensor(X, device="cuda")
     Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
     Uh = torch.zeros(n * dim, dtype=torch.float32).pin_memory()
     mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
@@ -485,6 +489,7 @@ def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, in
         f = np.stack([t.double().cpu().numpy() for t in f_t])
         assert cases.rel_err(f, f_ref) <= MIXED_TOL
         assert cases.rel_err(Uh.double().numpy(), U_ref) <= MIXED_TOL
+        assert np.array_equal(X_t.cpu().numpy(), Xc)
 
     plan.step_io(**io)
     torch.cuda.synchronize()
