@@ -68,3 +68,42 @@ def test_batched_graph_replay_matches_oracle(batch_mod, oracle):
     torch.cuda.synchronize()
     check_against_oracle(oracle, B, moved, F, u)
     B.close()
+
+
+def test_batched_graph_with_host_transfers_matches_oracle(batch_mod, oracle):
+    """One CUDA graph per step holding the host transfers (ibx_plan_step_io):
+    positions read by the binning straight from pinned host memory across
+    all problems, forces uploaded beside the binning, velocities downloaded
+    beside the spread.  Replayed with new host positions and forces, every
+    problem matches the oracle and the device position array follows the
+    host one."""
+    rng = np.random.default_rng(405)
+    problems = make_problems(rng, 24)
+    B = batch_mod.BatchedProblems(problems, dim=2, kernel="IB_4", tune=False)
+    nm = int(B.marker_offsets[-1])
+    u = [rng.standard_normal((2, N[1], N[0])) for N, _ in problems]
+    for k in range(len(problems)):
+        for a, t in enumerate(B.grid("u", k)):
+            t.copy_(torch.tensor(u[k][a], dtype=torch.float32))
+    Xh = B.X.cpu().pin_memory()
+    Fh = torch.zeros(nm * 2, dtype=torch.float32).pin_memory()
+    Uh = torch.zeros(nm * 2, dtype=torch.float32).pin_memory()
+    B.capture(B.host_io(Xh, Fh, Uh))
+    for rep in range(2):
+        # move every marker a little and draw new forces, on the host
+        X = Xh.numpy().reshape(-1, 2) + rng.uniform(-2e-3, 2e-3, size=(nm, 2))
+        X = np.mod(X, 1.0)
+        F = rng.standard_normal(nm * 2)
+        Xh.copy_(torch.tensor(X.reshape(-1)))
+        Fh.copy_(torch.tensor(F, dtype=torch.float32))
+        B.f.zero_()
+        torch.cuda.synchronize()
+        B.replay()
+        torch.cuda.synchronize()
+        assert B.status() == 0
+        assert np.array_equal(B.X.cpu().numpy(), Xh.numpy())
+        B.U.copy_(Uh)  # the downloaded velocities, checked like the device ones
+        moved = [(N, X[B.marker_offsets[k]: B.marker_offsets[k + 1]].reshape(-1)) for k, (N, _) in
+                 enumerate(problems)]
+        check_against_oracle(oracle, B, moved, F, u)
+    B.close()
