@@ -789,13 +789,14 @@ def nested(line):
     return {k: line[k] for k in NESTED_KEYS if k in line}
 
 
-def fortran_abi_case(dev, reps=5):
+def fortran_abi_case(dev, reps=7):
     """The reference's own entry points, called as LEInteractor calls them:
     lagrangian_ib_4_spread3d_ and lagrangian_ib_4_interp3d_ (the Fortran ABI
     of libibx) on one ghosted 128^3 cell patch of depth 3 with 200,000
     markers, every array a host array (staged through the library's pool,
     copied in and back per call), against the same calls with device
-    arrays.  One step = one spread + one interpolation."""
+    arrays.  One step = one spread + one interpolation; the median of the
+    separately timed calls."""
     import ctypes
 
     import numpy as np
@@ -828,13 +829,17 @@ def fortran_abi_case(dev, reps=5):
                                     pt(XX), pt(VV))
 
     def wall(arrs):
+        # the median of separately timed calls: one call disturbed by
+        # something else on the machine does not move it
         step(arrs)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        times = []
         for _ in range(reps):
+            t0 = time.perf_counter()
             step(arrs)
-        torch.cuda.synchronize()
-        return (time.perf_counter() - t0) / reps * 1e3
+            torch.cuda.synchronize()
+            times.append((time.perf_counter() - t0) * 1e3)
+        return float(np.median(times))
 
     host = (u, X, V.copy(), idx, sh)
     devs = tuple(torch.tensor(a, device=dev) for a in host)
