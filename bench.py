@@ -12,8 +12,9 @@ rate with host buffers and the roofline of the dominant kernel are reported
 on the same JSON line, and nested objects carry the other measured
 configurations: ``ib6`` (the same workload with IB_6), ``batched`` (512
 independent 2D problems, one CUDA graph per step, autotuned), ``serving``
-(Poisson request stream over resident simulations, p50/p99 latency) and
-``fortran_abi`` (the reference's Fortran entry points with host arrays).
+(Poisson request stream over resident simulations, p50/p99 latency),
+``fortran_abi`` (the reference's Fortran entry points with host arrays) and
+``kernels`` (IB_3, PIECEWISE_CUBIC and BSPLINE_4 on the 2M-marker workload).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                   [--workload all|helices|batched|serving] [--kernel K]
@@ -886,6 +887,12 @@ def run_ours(args):
             line["batched"] = nested(batched_case(args, dev, world, with_cpu, args.steps, args.warmup))
             line["serving"] = nested(serving_case(args, dev, world, with_cpu, args.steps))
             line["fortran_abi"] = fortran_abi_case(dev)
+            # the other kernels of the path on the same workload (autotuned, no CPU baseline)
+            line["kernels"] = {k: {key: v for key, v in helices_case(args, k, dev, world, "tune", False, args.steps,
+                                                                     args.warmup).items()
+                                   if key in ("value", "unit", "ms_per_step", "phases_ms", "mixed_vs_plain",
+                                              "error_vs_fp64", "roofline", "e2e", "status")}
+                               for k in ("IB_3", "PIECEWISE_CUBIC", "BSPLINE_4")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -315,20 +315,27 @@ ib3_f(float r)
     if (r < 1.5f) return 0.16666666666667f * (5.f - 3.f * r - sqrt_f32(1.f - 3.f * (1.f - r) * (1.f - r)));
     return 0.f;
 }
+// The cubic B-spline of FDELTA:268-294 in the same pieces (|x| <= 1,
+// |x| <= 2), written in |x| itself: the reference's polynomials in
+// r = |x| + 2 (FP64 path, ibx_device.cuh) expand to (4 - 6 x^2 + 3 |x|^3) / 6
+// and (2 - |x|)^3 / 6, which FP32 evaluates without the cancellation of terms
+// of size ~200 that the r form suffers.
 __device__ __forceinline__ float
 bspline4_f(float x)
 {
-    const float modx = fabsf(x);
-    const float r = modx + 2.f;
-    const float r2 = r * r;
-    const float r3 = r2 * r;
-    if (modx <= 1.f) return (1.f / 6.f) * (3.f * r3 - 24.f * r2 + 60.f * r - 44.f);
-    if (modx <= 2.f) return (1.f / 6.f) * (-r3 + 12.f * r2 - 48.f * r + 64.f);
+    const float m = fabsf(x);
+    if (m <= 1.f) return (2.f / 3.f) - m * m + 0.5f * (m * m * m);
+    if (m <= 2.f)
+    {
+        const float t = 2.f - m;
+        return (1.f / 6.f) * (t * t * t);
+    }
     return 0.f;
 }
 
 // The W weights of one dimension from r_first; the formulas of the FP64
-// path (ibx_device.cuh) evaluated in FP32.
+// path (ibx_device.cuh) evaluated in FP32 (the B-spline in an equal,
+// better-conditioned form).
 template <int K>
 __device__ __forceinline__ void
 weights_f32(float rf, float* w)
