@@ -347,6 +347,25 @@ def tile_index(X, N, edges):
     return t
 
 
+def capture_step(fn):
+    """Capture fn (one step's launches on the current stream) into a CUDA
+    graph; returns (graph, libibx kernels launched per step)."""
+    import torch
+
+    from ibamr_gb300 import ibx
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    k0 = ibx.kernel_launches()
+    with torch.cuda.graph(g, stream=s):
+        fn()
+    per_step = ibx.kernel_launches() - k0
+    torch.cuda.synchronize()
+    return g, per_step
+
+
 def pick_io_mode(plan, step_e2e, timed, steps, recapture=None):
     """Step mode of the end-to-end step (bin + spread + interpolate with
     their host transfers): the plan's own mode, or mode 0 (interpolation
@@ -427,8 +446,15 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
         if world > 1:
             torch.distributed.barrier()
 
+    # One step (bin, then spread and interpolate concurrently) captured once
+    # into a CUDA graph and replayed, as a time stepper runs it; the kernels
+    # of a replay are the ones counted at capture.
     for _ in range(warmup):
         plan.step()
+    torch.cuda.synchronize()
+    graph, per_step = capture_step(lambda: plan.step())
+    for _ in range(warmup):
+        graph.replay()
     torch.cuda.synchronize()
     sampler = ClockSampler(dev.index or 0)
     sampler.start()
@@ -436,15 +462,15 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    launches0 = ibx.kernel_launches()
     torch.cuda.nvtx.range_push("timed_steps")  # profilers can select the timed launches by this range
     e0.record(stream)
     for _ in range(steps):
-        plan.step()  # bin, then spread and interpolate concurrently
+        graph.replay()
     e1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    launches = ibx.kernel_launches() - launches0
+    launches = per_step * steps
+    del graph
     barrier()
     clocks = sampler.stop()
     ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, dev)
@@ -529,21 +555,30 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
     Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
     Uh = torch.empty(3 * n, dtype=torch.float32).pin_memory()
     io = dict(in_X=[(X_t, Xh)], in_Q=[(F_t, Fh)], out_Q=[(Uh, U_t)])
+    io_graph = [None]
+
+    def recapture():
+        io_graph[0] = None
+        plan.step_io(**io)
+        torch.cuda.synchronize()
+        io_graph[0] = capture_step(lambda: plan.step_io(**io))[0]
 
     def step_e2e():
-        plan.step_io(**io)
+        io_graph[0].replay()
 
-    # the step mode of the transfer step: the tuned one, or the interpolation
-    # first with the velocities' copy beside the spread, whichever is faster
-    io_mode = pick_io_mode(plan, step_e2e, timed, steps)
+    # the step mode of the transfer step (one CUDA graph holding the
+    # transfers): the tuned one, or the interpolation first with the
+    # velocities' copy beside the spread, whichever is faster
+    io_mode = pick_io_mode(plan, step_e2e, timed, steps, recapture=recapture)
 
     for _ in range(2):
         step_e2e()
     barrier()
     ms_e2e = max_over_ranks(timed(step_e2e, steps), world, dev)
     e2e = {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": X.size * 8 + F.size * 4,
-           "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e, "call": "ibx_plan_step_io",
+           "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e, "call": "ibx_plan_step_io (in the graph)",
            "step_mode": io_mode}
+    io_graph[0] = None
     status = plan.status()
     tile_edges = list(plan.tile_shape[1])
     plan.close()
@@ -557,7 +592,8 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
         "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded)",
         "config": {"workload": workload, "markers": n, "grid": N, "kernel": kernel, "centering": "side",
-                   "precision": "mixed", "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
+                   "precision": "mixed", "launch": "one CUDA graph per step",
+                   "l2": "inputs larger than L2 (2 x 201 MB grids, 72 MB markers)",
                    "parallelism": "replicas" if world > 1 else "single"},
         "phases_ms": {"bin": t_bin, "spread": t_spread, "interpolate": t_interp},
         "plain_fp64": {"value": world * n / (ms_plain * 1e-3), "ms_per_step": ms_plain,
