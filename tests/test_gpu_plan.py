@@ -518,6 +518,39 @@ def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, in
     plan.close()
 
 
+def test_step_io_several_transfers_per_list(ibx, oracle):
+    """Positions and forces in two transfers each (halves of the arrays) and
+    the velocities out in two: the copy path of ibx_plan_step_io, against
+    the oracle."""
+    rng = np.random.default_rng(171)
+    dim, N, n = 3, [24, 20, 16], 3001
+    X = seam_markers(rng, n, dim)
+    F = rng.standard_normal(n * dim)
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    X_t = torch.zeros(n * dim, dtype=torch.float64, device="cuda")
+    f_t = [torch.zeros(list(N)[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    F_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    Xh = torch.tensor(X).pin_memory()
+    Fh = torch.tensor(F, dtype=torch.float32).pin_memory()
+    Uh = torch.zeros(n * dim, dtype=torch.float32).pin_memory()
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), "IB_4", ibx.MIXED, interp_problems=[mk(u_t, U_t)])
+    h = (n // 2) * dim
+    plan.step_io(in_X=[(X_t[:h], Xh[:h]), (X_t[h:], Xh[h:])], in_Q=[(F_t[:h], Fh[:h]), (F_t[h:], Fh[h:])],
+                 out_Q=[(Uh[:h], U_t[:h]), (Uh[h:], U_t[h:])])
+    torch.cuda.synchronize()
+    assert plan.status() == ibx.OK
+    f_ref, U_ref = oracle.periodic_problem(dim, N, "IB_4", X, F=F, u=u, centering=1)
+    f = np.stack([t.double().cpu().numpy() for t in f_t])
+    assert cases.rel_err(f, f_ref) <= MIXED_TOL
+    assert cases.rel_err(Uh.double().numpy(), U_ref) <= MIXED_TOL
+    assert np.array_equal(X_t.cpu().numpy(), X)
+    plan.close()
+
+
 @pytest.mark.parametrize("form", [1, 2, 3])
 @pytest.mark.parametrize("tile_shape", [0, 1])
 @pytest.mark.parametrize("kernel", KERNEL_NAMES)
