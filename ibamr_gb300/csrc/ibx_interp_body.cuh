@@ -213,8 +213,8 @@ units_item(const DevPlan& D, int item, int* s_order, int* s_start)
         const int p = D.n_probs == 1 ? 0 : find_in_offsets(D.tile_offs, D.n_probs, t);
         const PlanProb& P = D.probs[p];
         const int ncomp = P.ncomp;
-        const int u0 = D.hucount[t] + k * D.item_units;
-        const int nu = max(0, min(D.item_units, D.hucount[t + 1] - u0));
+        int u0, nu;
+        item_unit_range(D, t, k, u0, nu);
         float* Qi = static_cast<float*>(P.Qi);
         const long long n0 = P.N[0], n01 = (long long)P.N[0] * P.N[1];
         // the item's units, longest first, as in the dense spread

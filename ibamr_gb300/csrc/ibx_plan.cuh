@@ -245,6 +245,19 @@ bool fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx);
 int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s,
                  cudaEvent_t records_done = nullptr, cudaEvent_t records_done2 = nullptr);
 
+// Home units [u0, u0 + nu) of dense work item k of tile t: the tile's units
+// split evenly over its items (ceil(units / item_units) items, so at most
+// item_units each), which keeps the longest item short.
+__device__ __forceinline__ void
+item_unit_range(const DevPlan& D, int t, int k, int& u0, int& nu)
+{
+    const int ub = D.hucount[t], ut = D.hucount[t + 1] - ub;
+    const int ni = D.items[t + 1] - D.items[t];
+    const int a = (int)((long long)ut * k / ni), b = (int)((long long)ut * (k + 1) / ni);
+    u0 = ub + a;
+    nu = b - a;
+}
+
 template <typename T>
 __device__ __forceinline__ int
 find_in_offsets(const T* offs, int n, T g)

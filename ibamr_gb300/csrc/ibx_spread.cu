@@ -166,8 +166,8 @@ dense_item(const DevPlan& D, int item, float* sm)
         // similar length and finish together.
         __shared__ int s_order[MAX_ITEM_UNITS];
         __shared__ int s_start[33];
-        const int u0 = D.hucount[t] + k * D.item_units;
-        const int nu = max(0, min(D.item_units, D.hucount[t + 1] - u0));
+        int u0, nu;
+        item_unit_range(D, t, k, u0, nu);
         if (RG::regs)
         {
             if (threadIdx.x < 33) s_start[threadIdx.x] = 0;
