@@ -136,18 +136,34 @@ agg_count(int* counters, int key, bool valid)
     }
 }
 
-// Distinct tiles (along one dim) holding the cells (b+i) mod N, i in [0, span).
+// Distinct tiles (along one dim, at most 4, in order of first appearance)
+// holding the cells (b+i) mod N, i in [0, span), span <= MAXSPAN; unrolled,
+// with the list in registers (no dynamic indexing).
+template <int MAXSPAN, int E>
 __device__ __forceinline__ int
-tiles_1d(int b, int span, int N, int E, int* out)
+tiles_1d(int b, int span, int N, int* out)
 {
-    int n = 0;
-    for (int i = 0; i < span; ++i)
+    int o0 = 0, o1 = 0, o2 = 0, o3 = 0, n = 0;
+#pragma unroll
+    for (int i = 0; i < MAXSPAN; ++i)
     {
+        if (i >= span) break;
         const int tile = wrap_from_base(b + i, N) / E;
-        bool seen = false;
-        for (int k = 0; k < n; ++k) seen = seen || out[k] == tile;
-        if (!seen && n < 4) out[n++] = tile;
+        const bool seen = (n > 0 && o0 == tile) || (n > 1 && o1 == tile) || (n > 2 && o2 == tile) ||
+                          (n > 3 && o3 == tile);
+        if (!seen && n < 4)
+        {
+            o0 = n == 0 ? tile : o0;
+            o1 = n == 1 ? tile : o1;
+            o2 = n == 2 ? tile : o2;
+            o3 = n == 3 ? tile : o3;
+            ++n;
+        }
     }
+    out[0] = o0;
+    out[1] = o1;
+    out[2] = o2;
+    out[3] = o3;
     return n;
 }
 
@@ -163,25 +179,47 @@ visit_tiles(const PlanProb& P, const Rec& R, int (*tl)[4], int* nt)
         if (d >= DIM)
         {
             nt[d] = 1;
-            tl[d][0] = 0;
+            tl[d][0] = tl[d][1] = tl[d][2] = tl[d][3] = 0;
             continue;
         }
         const int lo = R.bc(d);
-        const int hi = R.bc(d) + (P.side ? R.stagger(d) : 0) + W - 1;
-        nt[d] = tiles_1d(lo, hi - lo + 1, P.N[d], TileT<DIM, SH>::edge(d), tl[d]);
+        const int span = (P.side ? R.stagger(d) : 0) + W;
+        nt[d] = d == 0   ? tiles_1d<W + 1, TileT<DIM, SH>::E0>(lo, span, P.N[d], tl[d])
+                : d == 1 ? tiles_1d<W + 1, TileT<DIM, SH>::E1>(lo, span, P.N[d], tl[d])
+                         : tiles_1d<W + 1, TileT<DIM, SH>::E2>(lo, span, P.N[d], tl[d]);
         total *= nt[d];
     }
     return total;
 }
 
+__device__ __forceinline__ int
+pick4(const int* a, int i)
+{
+    return i == 0 ? a[0] : i == 1 ? a[1] : i == 2 ? a[2] : a[3];
+}
+
+// The tile of the visit whose per-dim tile digits are c (c[0] fastest).
 template <int DIM>
 __device__ __forceinline__ int
-visit_tile_id(const PlanProb& P, int (*tl)[4], const int* nt, int k)
+visit_tile_at(const PlanProb& P, int (*tl)[4], const int* c)
 {
-    const int c0 = k % nt[0];
-    const int c1 = (k / nt[0]) % nt[1];
-    const int c2 = DIM == 3 ? k / (nt[0] * nt[1]) : 0;
-    return P.tile0 + tl[0][c0] + P.ntile[0] * (tl[1][c1] + P.ntile[1] * tl[2][c2]);
+    return P.tile0 + pick4(tl[0], c[0]) +
+           P.ntile[0] * (pick4(tl[1], c[1]) + (DIM == 3 ? P.ntile[1] * pick4(tl[2], c[2]) : 0));
+}
+
+// The next visit's digits: a mixed-radix counter over nt (no divisions).
+__device__ __forceinline__ void
+visit_next(int* c, const int* nt)
+{
+    if (++c[0] == nt[0])
+    {
+        c[0] = 0;
+        if (++c[1] == nt[1])
+        {
+            c[1] = 0;
+            ++c[2];
+        }
+    }
 }
 
 // The stencil bases of a record as one 64-bit key: markers with equal keys
@@ -356,10 +394,12 @@ __global__ void __launch_bounds__(256) scatter_home_kernel(const DevPlan D)
             if (!dense_home(D, ht)) nvis = visit_tiles<DIM, K, SH>(P, R, tl, nt);
         }
     }
+    int cd[3] = { 0, 0, 0 };
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
-        agg_count(D.vcount, v ? visit_tile_id<DIM>(P, tl, nt, k) : 0, v);
+        agg_count(D.vcount, v ? visit_tile_at<DIM>(P, tl, cd) : 0, v);
+        if (v) visit_next(cd, nt);
     }
 }
 
@@ -375,10 +415,12 @@ __global__ void __launch_bounds__(256) scatter_visits_kernel(const DevPlan D)
     const PlanProb& P = D.probs[p];
     int tl[3][4], nt[3] = { 0, 0, 0 }, nvis = 0;
     if (valid) nvis = visit_tiles<DIM, K, SH>(P, D.rec[g], tl, nt);
+    int cd[3] = { 0, 0, 0 };
     for (int k = 0; __any_sync(0xffffffffu, k < nvis); ++k)
     {
         const bool v = k < nvis;
-        const int t = v ? visit_tile_id<DIM>(P, tl, nt, k) : 0;
+        const int t = v ? visit_tile_at<DIM>(P, tl, cd) : 0;
+        if (v) visit_next(cd, nt);
         const unsigned act = __ballot_sync(0xffffffffu, v);
         if (v)
         {
