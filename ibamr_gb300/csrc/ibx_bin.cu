@@ -618,8 +618,14 @@ launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 }
 
 int
+launch_visits(int dim, int kernel, const DevPlan& D, cudaStream_t s)
+{
+    return launch_bin(dim, kernel, D, s, 2);
+}
+
+int
 bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s, cudaEvent_t records_done,
-             cudaEvent_t records_done2)
+             cudaEvent_t records_done2, bool defer_visits)
 {
     const int nt = D.n_tiles;
     // Counters, cursors and item counts are contiguous: one memset.
@@ -630,8 +636,8 @@ bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t 
     if (!rc) rc = exclusive_scan(D.hcount, nt + 1, 2, scan_tmp, s); // hcount, hucount
     if (!rc) rc = launch_bin(dim, kernel, D, s, 1);                 // also counts the work items
     if (!rc) rc = exclusive_scan(D.vcount, nt + 1, 2, scan_tmp, s); // vcount, items
-    if (!rc) rc = launch_bin(dim, kernel, D, s, 2);
     if (!rc) rc = launch_items_fill(D, s);
+    if (!rc && !defer_visits) rc = launch_bin(dim, kernel, D, s, 2);
     return rc;
 }
 

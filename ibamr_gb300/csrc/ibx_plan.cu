@@ -158,6 +158,10 @@ struct ibx_plan
     // the caller's stream (0)
     cudaStream_t side, spread_s;
     cudaEvent_t ev_fork, ev_join, ev_join2;
+    // the visit placement, deferred out of the binning to run beside the
+    // dense-tile spread and the interpolation; the per-visit spread waits
+    // for it
+    cudaEvent_t ev_vis;
     // ibx_plan_step_io: the spread values' upload runs on `up`, behind the
     // positions' upload on the caller's stream (ev_x), and the spread waits
     // for it (ev_q)
@@ -346,6 +350,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
         cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_join2, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&plan->ev_vis, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithPriority(&plan->up, cudaStreamNonBlocking, greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_x, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_q, cudaEventDisableTiming) != cudaSuccess)
@@ -447,8 +452,12 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     // concurrent mode it forks as soon as they exist, beside the counting
     // sort; the other forms fork after the whole binning.
     const bool early = plan->step_mode == 1 && plan->D.interp_form == 2;
+    // the visit placement is left out of the binning in the two-launch
+    // modes: it runs beside the dense-tile spread and the interpolation,
+    // which do not read the visits
+    const bool defer = plan->step_mode != 2;
     rc = bin_sequence(plan->dim, plan->kernel, D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr,
-                      up && direct ? plan->ev_x : nullptr);
+                      up && direct ? plan->ev_x : nullptr, defer);
     if (up && direct)
     {
         const int ru = rc ? IBX_OK : upload();
@@ -470,27 +479,29 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     }
     if (plan->step_mode == 0)
     {
-        // the interpolation first, its values copied out on `side` while the
-        // spread runs
+        // the visits placed on `side` while the interpolation runs first;
+        // the interpolated values are copied out on `side` while the spread
+        // runs
+        const bool vf = cudaEventRecord(plan->ev_join2, s) == cudaSuccess &&
+                        cudaStreamWaitEvent(plan->side, plan->ev_join2, 0) == cudaSuccess;
+        int rv = launch_visits(plan->dim, plan->kernel, plan->D, vf ? plan->side : s);
+        if (vf && cudaEventRecord(plan->ev_vis, plan->side) != cudaSuccess) rv = rv ? rv : IBX_E_CUDA;
         rc = launch_interp(plan->dim, plan->kernel, plan->D, s);
-        bool forked = false;
         if (!rc && out)
         {
-            if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess ||
+            if (!vf || cudaEventRecord(plan->ev_fork, s) != cudaSuccess ||
                 cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
                 rc = IBX_E_CUDA;
             else
-            {
-                forked = true;
                 rc = copy_all(out_Q, n_out_Q, plan->side);
-            }
         }
         if (!wait_up(s)) rc = rc ? rc : IBX_E_CUDA;
-        if (!rc) rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
-        if (forked && (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
-                       cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess))
+        if (!rc && !rv) rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s, vf ? plan->ev_vis : nullptr);
+        // join `side` (visits, copy) even after a failure
+        if (vf && (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
+                   cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess))
             rc = rc ? rc : IBX_E_CUDA;
-        return rc;
+        return rc ? rc : rv;
     }
     // spread and interpolation read the same records and write different
     // arrays: they overlap on the device.  The longer phase, the spread, runs
@@ -510,9 +521,13 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
         wait_up(s);
         return IBX_E_CUDA;
     }
+    // the visits placed on the caller's stream beside both phases; the
+    // per-visit spread waits for them
+    int rv = launch_visits(plan->dim, plan->kernel, plan->D, s);
+    if (!rv && cudaEventRecord(plan->ev_vis, s) != cudaSuccess) rv = IBX_E_CUDA;
     rc = launch_interp(plan->dim, plan->kernel, plan->D, s_int);
     if (!rc) rc = copy_all(out_Q, n_out_Q, s_int);
-    const int rs = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s_spr);
+    const int rs = rv ? rv : launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s_spr, plan->ev_vis);
     // join even after a failed launch, so that no stream of the plan is left forked
     if (cudaEventRecord(plan->ev_join, s_int) != cudaSuccess || cudaEventRecord(plan->ev_join2, s_spr) != cudaSuccess ||
         cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess || cudaStreamWaitEvent(s, plan->ev_join2, 0) != cudaSuccess)
@@ -715,6 +730,7 @@ ibx_plan_destroy(ibx_plan* plan)
     cudaEventDestroy(plan->ev_fork);
     cudaEventDestroy(plan->ev_join);
     cudaEventDestroy(plan->ev_join2);
+    cudaEventDestroy(plan->ev_vis);
     cudaEventDestroy(plan->ev_x);
     cudaEventDestroy(plan->ev_q);
     const cudaError_t e = cudaFree(plan->dmem);

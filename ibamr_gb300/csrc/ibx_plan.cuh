@@ -237,13 +237,16 @@ PlanCarve carve_plan(const PlanSizes& z, char* base, DevPlan& D);
 // when the problem's coordinate range does not fit it.
 bool fixed_dim(double x_lower, double x_upper, double dx, FixedDim& fx);
 
-// The binning sequence of one step (counters zeroed, bin, scans, scatters,
-// dense work items).
-// Binning of a plan on stream s; records_done and records_done2 (optional)
-// are recorded once the stencil records and home tiles exist (before the
-// counting sort).
+// The binning sequence of one step (counters zeroed, bin, scans, home
+// placement, dense work items, visit placement) on stream s; records_done
+// and records_done2 (optional) are recorded once the stencil records and
+// home tiles exist (before the counting sort).  defer_visits: the visit
+// placement is left out, for the caller to launch (launch_visits) beside the
+// kernels that do not read the visits (the dense-tile spread, the
+// interpolation).
 int bin_sequence(int dim, int kernel, const DevPlan& D, int* scan_tmp, cudaStream_t s,
-                 cudaEvent_t records_done = nullptr, cudaEvent_t records_done2 = nullptr);
+                 cudaEvent_t records_done = nullptr, cudaEvent_t records_done2 = nullptr,
+                 bool defer_visits = false);
 
 // Home units [u0, u0 + nu) of dense work item k of tile t: the tile's units
 // split evenly over its items (ceil(units / item_units) items, so at most
@@ -417,7 +420,13 @@ int launch_bin(int dim, int kernel, const DevPlan& D, cudaStream_t s, int phase)
 // holds count * 2048 ints.
 int exclusive_scan(int* data, int n, int count, int* tmp, cudaStream_t s);
 int launch_items_fill(const DevPlan& D, cudaStream_t s);
-int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);
+// The visit placement (launch_bin phase 2) of a binning run with
+// defer_visits.
+int launch_visits(int dim, int kernel, const DevPlan& D, cudaStream_t s);
+// The dense-tile spread, then the per-visit spread; visits_done (optional):
+// an event the per-visit kernel waits for (the deferred visit placement).
+int launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s,
+                  cudaEvent_t visits_done = nullptr);
 // Spread and interpolation of the binned markers in one persistent launch
 // (ibx_spread.cu: step_fused).
 int launch_fused(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s);

@@ -1137,7 +1137,7 @@ launch_gather(const DevPlan& D, cudaStream_t s, int sms)
 
 template <int DIM, int K, int SH>
 int
-launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
+launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms, cudaEvent_t visits_done)
 {
     constexpr int W = KT<K>::W;
     const int per_sm = D.dense_blocks_per_sm > 0 ? D.dense_blocks_per_sm : 2;
@@ -1153,6 +1153,7 @@ launch_spread_k(const DevPlan& D, int max_ncomp, cudaStream_t s, int sms)
         note_launches(1);
         if (cudaGetLastError() != cudaSuccess) return IBX_E_CUDA;
     }
+    if (visits_done && cudaStreamWaitEvent(s, visits_done, 0) != cudaSuccess) return IBX_E_CUDA;
     if (D.visit_kernel == 2 || D.visit_kernel == 3)
     {
         constexpr int OCC = GatherOccupancy<DIM, SH>::value;
@@ -1214,7 +1215,7 @@ launch_fused(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t 
 }
 
 int
-launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s)
+launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t s, cudaEvent_t visits_done)
 {
     if (D.n_tiles == 0) return IBX_OK;
     if (cudaMemsetAsync(D.work, 0, 2 * sizeof(int), s) != cudaSuccess) return IBX_E_CUDA;
@@ -1224,7 +1225,8 @@ launch_spread(int dim, int kernel, const DevPlan& D, int max_ncomp, cudaStream_t
     const int sh = D.tile_shape;
 #define IBX_SPREAD_CASE(DD, KK)                                                                                      \
     if (dim == DD && kernel == KK)                                                                                   \
-        return sh == 0 ? launch_spread_k<DD, KK, 0>(D, max_ncomp, s, sms) : launch_spread_k<DD, KK, 1>(D, max_ncomp, s, sms);
+        return sh == 0 ? launch_spread_k<DD, KK, 0>(D, max_ncomp, s, sms, visits_done)                             \
+                       : launch_spread_k<DD, KK, 1>(D, max_ncomp, s, sms, visits_done);
     IBX_SPREAD_CASE(2, K_PL) IBX_SPREAD_CASE(2, K_PCUBIC) IBX_SPREAD_CASE(2, K_IB3) IBX_SPREAD_CASE(2, K_IB4)
     IBX_SPREAD_CASE(2, K_IB6) IBX_SPREAD_CASE(2, K_BSPL4) IBX_SPREAD_CASE(3, K_PL) IBX_SPREAD_CASE(3, K_PCUBIC)
     IBX_SPREAD_CASE(3, K_IB3) IBX_SPREAD_CASE(3, K_IB4) IBX_SPREAD_CASE(3, K_IB6) IBX_SPREAD_CASE(3, K_BSPL4)
