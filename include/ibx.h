@@ -361,7 +361,10 @@ int ibx_plan_bin(ibx_plan* plan, void* stream);
  * concurrently (they read the same bins and write different arrays; the
  * spread's stream has the device's greatest priority, the interpolation's
  * the least, so the longer phase gets the SMs first), both joined back into
- * `stream` before the call's work ends.  Graph-capturable like the others. */
+ * `stream` before the call's work ends.  The binning's last kernel (the
+ * placement of the sparse-homed markers' visits) runs on `stream` beside
+ * them: only the per-visit spread waits for it.  Graph-capturable like the
+ * others. */
 int ibx_plan_step(ibx_plan* plan, void* stream);
 /* One copy of ibx_plan_step_io: `bytes` bytes from src to dst, either of
  * them host or device memory (cudaMemcpyDefault).  Host buffers must be
