@@ -347,25 +347,6 @@ def tile_index(X, N, edges):
     return t
 
 
-def capture_step(fn):
-    """Capture fn (one step's launches on the current stream) into a CUDA
-    graph; returns (graph, libibx kernels launched per step)."""
-    import torch
-
-    from ibamr_gb300 import ibx
-
-    s = torch.cuda.Stream()
-    s.wait_stream(torch.cuda.current_stream())
-    torch.cuda.synchronize()
-    g = torch.cuda.CUDAGraph()
-    k0 = ibx.kernel_launches()
-    with torch.cuda.graph(g, stream=s):
-        fn()
-    per_step = ibx.kernel_launches() - k0
-    torch.cuda.synchronize()
-    return g, per_step
-
-
 def pick_io_mode(plan, step_e2e, timed, steps, recapture=None):
     """Step mode of the end-to-end step (bin + spread + interpolate with
     their host transfers): the plan's own mode, or mode 0 (interpolation
@@ -447,14 +428,16 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
             torch.distributed.barrier()
 
     # One step (bin, then spread and interpolate concurrently) captured once
-    # into a CUDA graph and replayed, as a time stepper runs it; the kernels
-    # of a replay are the ones counted at capture.
+    # into a CUDA graph that keeps the plan's stream priorities
+    # (ibx_plan_graph) and replayed, as a time stepper runs it; the kernels of
+    # a replay are the ones counted at capture.
     for _ in range(warmup):
         plan.step()
     torch.cuda.synchronize()
-    graph, per_step = capture_step(lambda: plan.step())
+    graph = plan.graph()
+    per_step = graph.kernels
     for _ in range(warmup):
-        graph.replay()
+        graph.launch(stream)
     torch.cuda.synchronize()
     sampler = ClockSampler(dev.index or 0)
     sampler.start()
@@ -465,12 +448,12 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
     torch.cuda.nvtx.range_push("timed_steps")  # profilers can select the timed launches by this range
     e0.record(stream)
     for _ in range(steps):
-        graph.replay()
+        graph.launch(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     launches = per_step * steps
-    del graph
+    graph.close()
     barrier()
     clocks = sampler.stop()
     ms = max_over_ranks(e0.elapsed_time(e1) / steps, world, dev)
@@ -558,13 +541,15 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
     io_graph = [None]
 
     def recapture():
+        if io_graph[0] is not None:
+            io_graph[0].close()
         io_graph[0] = None
         plan.step_io(**io)
         torch.cuda.synchronize()
-        io_graph[0] = capture_step(lambda: plan.step_io(**io))[0]
+        io_graph[0] = plan.graph(**io)
 
     def step_e2e():
-        io_graph[0].replay()
+        io_graph[0].launch(stream)
 
     # the step mode of the transfer step (one CUDA graph holding the
     # transfers): the tuned one, or the interpolation first with the
@@ -578,6 +563,7 @@ def helices_case(args, kernel, dev, world, setting_mode, with_cpu, steps, warmup
     e2e = {"value": world * n / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": X.size * 8 + F.size * 4,
            "d2h_bytes_per_step": 3 * n * 4, "ms_per_step": ms_e2e, "call": "ibx_plan_step_io (in the graph)",
            "step_mode": io_mode}
+    io_graph[0].close()
     io_graph[0] = None
     status = plan.status()
     tile_edges = list(plan.tile_shape[1])

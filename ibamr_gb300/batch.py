@@ -81,9 +81,9 @@ class BatchedProblems:
         shape with its knobs; a captured graph is dropped."""
         from . import tuning
 
+        self._drop_graph()
         if self.plan is not None:
             self.plan.close()
-        self.graph = None
         self.plan = self._make(setting.get("tile_shape", 0))
         tuning.apply_setting(self.plan, setting)
 
@@ -94,9 +94,9 @@ class BatchedProblems:
         spread target ``f`` is zeroed afterwards; a captured graph is dropped."""
         from . import tuning
 
+        self._drop_graph()
         if self.plan is not None:
             self.plan.close()
-        self.graph = None
         self.plan, self.tuning = tuning.autotune_shape(self._make, reps=reps)
         self.f.zero_()
 
@@ -129,29 +129,33 @@ class BatchedProblems:
 
     def capture(self, io=None):
         """Capture one step (with the host transfers io, see step) into a
-        CUDA graph, after an eager warm-up step."""
+        CUDA graph that keeps the plan's stream priorities (Plan.graph),
+        after an eager warm-up step."""
         import torch
 
+        self._drop_graph()
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
             self.step(io)
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g):
-            self.step(io)
-        self.graph = g
-        return g
+        self.graph = self.plan.graph(**(io or {}))
+        return self.graph
 
-    def replay(self):
+    def replay(self, stream=None):
         if self.graph is None:
             self.capture()
-        self.graph.replay()
+        self.graph.launch(stream)
+
+    def _drop_graph(self):
+        if self.graph is not None:
+            self.graph.close()
+        self.graph = None
 
     def status(self):
         return self.plan.status()
 
     def close(self):
-        self.graph = None
+        self._drop_graph()
         self.plan.close()

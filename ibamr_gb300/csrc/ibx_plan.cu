@@ -157,6 +157,8 @@ struct ibx_plan
     // caller's stream (step_mode 1); or the spread then the interpolation on
     // the caller's stream (0)
     cudaStream_t side, spread_s;
+    // step_mode 3: the spread on `level`, of the interpolation's priority
+    cudaStream_t level;
     cudaEvent_t ev_fork, ev_join, ev_join2;
     // the visit placement, deferred out of the binning to run beside the
     // dense-tile spread and the interpolation; the per-visit spread waits
@@ -346,6 +348,7 @@ ibx_plan_create3(const ibx_problem* problems, const ibx_problem* interp_problems
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
         cudaStreamCreateWithPriority(&plan->side, cudaStreamNonBlocking, least) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&plan->level, cudaStreamNonBlocking, least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&plan->spread_s, cudaStreamNonBlocking, greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming) != cudaSuccess ||
@@ -451,11 +454,12 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     // Interpolation in marker order needs only the stencil records: in the
     // concurrent mode it forks as soon as they exist, beside the counting
     // sort; the other forms fork after the whole binning.
-    const bool early = plan->step_mode == 1 && plan->D.interp_form == 2;
-    // the visit placement is left out of the binning in the two-launch
+    const bool concurrent = plan->step_mode == 1 || plan->step_mode == 3;
+    const bool early = concurrent && plan->D.interp_form == 2;
+    // the visit placement is left out of the binning in the concurrent
     // modes: it runs beside the dense-tile spread and the interpolation,
     // which do not read the visits
-    const bool defer = plan->step_mode != 2;
+    const bool defer = concurrent;
     rc = bin_sequence(plan->dim, plan->kernel, D, plan->scan_tmp, s, early ? plan->ev_fork : nullptr,
                       up && direct ? plan->ev_x : nullptr, defer);
     if (up && direct)
@@ -479,37 +483,37 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     }
     if (plan->step_mode == 0)
     {
-        // the visits placed on `side` while the interpolation runs first;
-        // the interpolated values are copied out on `side` while the spread
-        // runs
-        const bool vf = cudaEventRecord(plan->ev_join2, s) == cudaSuccess &&
-                        cudaStreamWaitEvent(plan->side, plan->ev_join2, 0) == cudaSuccess;
-        int rv = launch_visits(plan->dim, plan->kernel, plan->D, vf ? plan->side : s);
-        if (vf && cudaEventRecord(plan->ev_vis, plan->side) != cudaSuccess) rv = rv ? rv : IBX_E_CUDA;
+        // the interpolation first, its values copied out on `side` while the
+        // spread runs
         rc = launch_interp(plan->dim, plan->kernel, plan->D, s);
+        bool forked = false;
         if (!rc && out)
         {
-            if (!vf || cudaEventRecord(plan->ev_fork, s) != cudaSuccess ||
+            if (cudaEventRecord(plan->ev_fork, s) != cudaSuccess ||
                 cudaStreamWaitEvent(plan->side, plan->ev_fork, 0) != cudaSuccess)
                 rc = IBX_E_CUDA;
             else
+            {
+                forked = true;
                 rc = copy_all(out_Q, n_out_Q, plan->side);
+            }
         }
         if (!wait_up(s)) rc = rc ? rc : IBX_E_CUDA;
-        if (!rc && !rv) rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s, vf ? plan->ev_vis : nullptr);
-        // join `side` (visits, copy) even after a failure
-        if (vf && (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
-                   cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess))
+        if (!rc) rc = launch_spread(plan->dim, plan->kernel, plan->D, plan->max_ncomp, s);
+        if (forked && (cudaEventRecord(plan->ev_join, plan->side) != cudaSuccess ||
+                       cudaStreamWaitEvent(s, plan->ev_join, 0) != cudaSuccess))
             rc = rc ? rc : IBX_E_CUDA;
-        return rc ? rc : rv;
+        return rc;
     }
     // spread and interpolation read the same records and write different
-    // arrays: they overlap on the device.  The longer phase, the spread, runs
-    // on the stream of greatest priority -- unless the interpolated values
-    // are copied out, then the interpolation does, so that the copy runs
-    // beside the rest of the spread instead of after it.
-    cudaStream_t s_int = out ? plan->spread_s : plan->side;
-    cudaStream_t s_spr = out ? plan->side : plan->spread_s;
+    // arrays: they overlap on the device.  Mode 1: the longer phase, the
+    // spread, runs on the stream of greatest priority -- unless the
+    // interpolated values are copied out, then the interpolation does, so
+    // that the copy runs beside the rest of the spread instead of after it.
+    // Mode 3: both on streams of the least priority.
+    const bool level = plan->step_mode == 3;
+    cudaStream_t s_int = level ? plan->side : out ? plan->spread_s : plan->side;
+    cudaStream_t s_spr = level ? plan->level : out ? plan->side : plan->spread_s;
     if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
         cudaStreamWaitEvent(s_int, plan->ev_fork, 0) != cudaSuccess)
         return wait_up(s) ? IBX_E_CUDA : IBX_E_CUDA;
@@ -552,6 +556,69 @@ ibx_plan_step_io(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx
     if (!plan || !transfers_ok(in_X, n_in_X) || !transfers_ok(in_Q, n_in_Q) || !transfers_ok(out_Q, n_out_Q))
         return IBX_E_ARG;
     return plan_step(plan, static_cast<cudaStream_t>(stream), in_X, n_in_X, in_Q, n_in_Q, out_Q, n_out_Q);
+}
+
+} // extern "C"
+
+// A step captured into an instantiated CUDA graph (ibx_plan_graph).
+struct ibx_graph
+{
+    cudaGraphExec_t exec;
+    int kernels;
+};
+
+extern "C" {
+
+int
+ibx_plan_graph(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
+               const ibx_transfer* out_Q, int n_out_Q, void* stream, ibx_graph** graph)
+{
+    if (graph) *graph = nullptr;
+    // the legacy default stream cannot be captured
+    if (!plan || !graph || !stream || !transfers_ok(in_X, n_in_X) || !transfers_ok(in_Q, n_in_Q) ||
+        !transfers_ok(out_Q, n_out_Q))
+        return IBX_E_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return IBX_E_CUDA;
+    const long long k0 = ibx_kernel_launches();
+    const int rc = plan_step(plan, s, in_X, n_in_X, in_Q, n_in_Q, out_Q, n_out_Q);
+    const long long kernels = ibx_kernel_launches() - k0;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &g); // ends the capture also after a failed step
+    if (rc || ec != cudaSuccess || !g)
+    {
+        if (g) cudaGraphDestroy(g);
+        return rc ? rc : IBX_E_CUDA;
+    }
+    // the kernels keep their streams' priorities (the spread's greatest)
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t ei = cudaGraphInstantiateWithFlags(&x, g, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return IBX_E_CUDA;
+    *graph = new ibx_graph{ x, (int)kernels };
+    return IBX_OK;
+}
+
+int
+ibx_graph_launch(ibx_graph* graph, void* stream)
+{
+    if (!graph) return IBX_E_ARG;
+    return cudaGraphLaunch(graph->exec, static_cast<cudaStream_t>(stream)) == cudaSuccess ? IBX_OK : IBX_E_CUDA;
+}
+
+int
+ibx_graph_kernels(const ibx_graph* graph)
+{
+    return graph ? graph->kernels : -1;
+}
+
+int
+ibx_graph_destroy(ibx_graph* graph)
+{
+    if (!graph) return IBX_OK;
+    const cudaError_t e = cudaGraphExecDestroy(graph->exec);
+    delete graph;
+    return e == cudaSuccess ? IBX_OK : IBX_E_CUDA;
 }
 
 int
@@ -656,7 +723,7 @@ ibx_plan_get_unit_cap(const ibx_plan* plan)
 int
 ibx_plan_set_step_mode(ibx_plan* plan, int mode)
 {
-    if (!plan || mode < 0 || mode > 2) return IBX_E_ARG;
+    if (!plan || mode < 0 || mode > 3) return IBX_E_ARG;
     plan->step_mode = mode;
     return IBX_OK;
 }
@@ -723,9 +790,11 @@ ibx_plan_destroy(ibx_plan* plan)
     if (!plan) return IBX_OK;
     cudaStreamSynchronize(plan->side);
     cudaStreamSynchronize(plan->spread_s);
+    cudaStreamSynchronize(plan->level);
     cudaStreamSynchronize(plan->up);
     cudaStreamDestroy(plan->side);
     cudaStreamDestroy(plan->spread_s);
+    cudaStreamDestroy(plan->level);
     cudaStreamDestroy(plan->up);
     cudaEventDestroy(plan->ev_fork);
     cudaEventDestroy(plan->ev_join);

@@ -98,6 +98,11 @@ def lib():
             T = ctypes.POINTER(Transfer)
             L.ibx_plan_step_io.argtypes = [ctypes.c_void_p, T, ctypes.c_int, T, ctypes.c_int, T, ctypes.c_int,
                                            ctypes.c_void_p]
+            L.ibx_plan_graph.argtypes = [ctypes.c_void_p, T, ctypes.c_int, T, ctypes.c_int, T, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+            L.ibx_graph_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+            L.ibx_graph_kernels.argtypes = [ctypes.c_void_p]
+            L.ibx_graph_destroy.argtypes = [ctypes.c_void_p]
             L.ibx_plan_tma_problems.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.argtypes = [ctypes.c_void_p]
             L.ibx_plan_scratch_bytes.restype = ctypes.c_longlong
@@ -464,6 +469,48 @@ def _transfers(pairs):
     return arr
 
 
+class Graph:
+    """A plan step captured into a CUDA graph by ibx_plan_graph (the plan's
+    stream priorities kept); launch() replays it on a stream."""
+
+    def __init__(self, plan, in_X=(), in_Q=(), out_Q=(), capture_stream=None):
+        import torch
+
+        s = capture_stream if capture_stream is not None else torch.cuda.Stream()
+        # the capture stream starts after the work already queued on the current one
+        s.wait_stream(torch.cuda.current_stream())
+        arrs = [_transfers(pairs) for pairs in (in_X, in_Q, out_Q)]
+        h = ctypes.c_void_p()
+        rc = lib().ibx_plan_graph(plan.h, arrs[0], len(in_X), arrs[1], len(in_Q), arrs[2], len(out_Q),
+                                  _stream_handle(s), ctypes.byref(h))
+        if rc:
+            raise IbxError(rc, "ibx_plan_graph")
+        self.h = h
+        self._keep = (plan, arrs, in_X, in_Q, out_Q)  # the buffers the graph addresses
+
+    @property
+    def kernels(self):
+        """Library kernels one launch runs."""
+        return int(lib().ibx_graph_kernels(self.h))
+
+    def launch(self, stream=None):
+        rc = lib().ibx_graph_launch(self.h, _stream_handle(stream))
+        if rc:
+            raise IbxError(rc, "ibx_graph_launch")
+
+    def close(self):
+        if self.h:
+            lib().ibx_graph_destroy(self.h)
+            self.h = None
+            self._keep = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Plan:
     """Binned spread/interpolate pipeline over fixed IBX_MODE_PERIODIC problems."""
 
@@ -513,6 +560,12 @@ class Plan:
                                     _stream_handle(stream))
         if rc:
             raise IbxError(rc, "ibx_plan_step_io")
+
+    def graph(self, in_X=(), in_Q=(), out_Q=(), capture_stream=None):
+        """One step (with the host transfers of step_io, if any) captured into
+        a CUDA graph that keeps the plan's stream priorities (Graph).  Close
+        the graph before the plan."""
+        return Graph(self, in_X, in_Q, out_Q, capture_stream)
 
     def spread(self, stream=None):
         rc = lib().ibx_plan_spread(self.h, _stream_handle(stream))

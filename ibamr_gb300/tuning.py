@@ -16,14 +16,16 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   home unit, all in chunks in marker order started beside the sort, or
   markers evaluated from their home tile's region staged in shared memory
   (all of them, or the dense-homed ones);
-* ``step_mode``: spread and interpolation concurrent, one after the other,
-  or fused into one persistent launch in ``step``.
+* ``step_mode``: spread and interpolation concurrent (the spread's stream
+  first, or both of one priority), one after the other, or fused into one
+  persistent launch in ``step``.
 
 The best setting depends on the marker distribution (clustered fibres favour
 regions, scattered markers favour visits), so it is measured: every
 candidate runs ``bin`` + ``spread`` on the plan's own data (the whole
 ``step``, interpolation included, when the plan has its own interpolation
-targets) and the fastest is kept.
+targets: captured with ``Plan.graph`` and replayed, as a time stepper runs
+it) and the fastest is kept.
 
 The tile shape is a property of a plan, chosen when it is created
 (``autotune_shape`` builds one plan per shape, tunes each, and keeps the
@@ -42,7 +44,7 @@ DEFAULT_CANDIDATES = {
     "dense_blocks_per_sm": (1, 2, 4),
     "visit_kernel": (0, 1, 2, 3),
     "interp_kernel": (0, 1, 2, 3, 4),
-    "step_mode": (1, 0, 2),
+    "step_mode": (1, 3, 0, 2),
     "unit_cap": (32, 16, 8),
 }
 
@@ -72,8 +74,9 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     per-visit kernel form; the dense-kernel knobs (``item_units``,
     ``dense_blocks_per_sm``, ``unit_cap``); for plans with their own
     interpolation targets, the interpolation form jointly with the step mode
-    (concurrent, serial or fused spread and interpolation), and, when that
-    changed them, the dense-kernel knobs once more.  Returns {"best": (item_units, dense_min,
+    (concurrent, serial or fused spread and interpolation), and then, under
+    each of the two fastest of those pairs, the split with the visit form and
+    the dense-kernel knobs once more.  Returns {"best": (item_units, dense_min,
     dense_blocks_per_sm), "visit_kernel": form, "interp_kernel": form or
     None, "step_mode": mode or None, "unit_cap": cap, "ms": t, "table":
     [((item_units, dense_min, dense_blocks_per_sm, visit_kernel,
@@ -103,9 +106,6 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     stream = torch.cuda.current_stream()
 
     def step():
-        if full:
-            plan.step()
-            return
         if include_bin:
             plan.bin()
         plan.spread()
@@ -114,7 +114,17 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
 
     def measure(cfg):
         apply(cfg)
-        table.append((cfg, _time(step, reps, stream)))
+        if full:
+            # a whole step runs as a time stepper runs it: replayed from a
+            # CUDA graph (eager launches order the concurrent streams
+            # differently and would rank the step modes otherwise)
+            g = plan.graph()
+            try:
+                table.append((cfg, _time(lambda: g.launch(stream), reps, stream)))
+            finally:
+                g.close()
+        else:
+            table.append((cfg, _time(step, reps, stream)))
 
     def best_cfg():
         return min(table, key=lambda r: r[1])
@@ -129,16 +139,23 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
         measure((iu, dm, bps, vk, ik0, sm0, cap))
     if full:
         iu, dm, bps, vk, _, _, cap = best_cfg()[0]
+        stage3 = len(table)
         for ik, sm in itertools.product(cand["interp_kernel"], cand["step_mode"]):
             measure((iu, dm, bps, vk, ik, sm, cap))
-        # the dense knobs again under the chosen interpolation form and step
-        # mode: beside a concurrent interpolation fewer dense CTAs can be
-        # best, one after the other more
-        _, dm, _, vk, ik, sm, _ = best_cfg()[0]
-        if (ik, sm) != (ik0, sm0):
-            for iu, bps, cap in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"],
-                                                  cand["unit_cap"]):
-                measure((iu, dm, bps, vk, ik, sm, cap))
+        # the spread knobs again under the two fastest interpolation forms and
+        # step modes: beside a concurrent interpolation fewer dense CTAs and
+        # another split between the spread kernels can be best, one after the
+        # other more
+        ranked = sorted(table[stage3:], key=lambda r: r[1])
+        pairs = list(dict.fromkeys((c[4], c[5]) for c, _ in ranked))[:2]
+        for ik, sm in pairs:
+            for dm2, vk2 in itertools.product(cand["dense_min"], cand["visit_kernel"]):
+                measure((iu, dm2, bps, vk2, ik, sm, cap))
+            _, dm2, _, vk2, _, _, _ = min((r for r in table if (r[0][4], r[0][5]) == (ik, sm)),
+                                          key=lambda r: r[1])[0]
+            for iu2, bps2, cap2 in itertools.product(cand["item_units"], cand["dense_blocks_per_sm"],
+                                                     cand["unit_cap"]):
+                measure((iu2, dm2, bps2, vk2, ik, sm, cap2))
     cfg, ms = best_cfg()
     apply(cfg)
     out = {"best": tuple(plan.tuning()), "ms": ms, "table": table, "config": cfg, "visit_kernel": cfg[3],

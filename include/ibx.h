@@ -392,6 +392,23 @@ typedef struct ibx_transfer
  * graph-capturable with page-locked host buffers. */
 int ibx_plan_step_io(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
                      const ibx_transfer* out_Q, int n_out_Q, void* stream);
+/* A step of ibx_plan_step_io (any counts 0: of ibx_plan_step) captured on
+ * `stream` into a CUDA graph and instantiated so that its kernels keep the
+ * priorities of the plan's streams (cudaGraphInstantiateFlagUseNodePriority:
+ * a graph instantiated without it runs every kernel at the priority of the
+ * stream it is launched into, and the spread then no longer comes first).
+ * No reference counterpart: the graph of a time stepper's step.  `stream`
+ * must not be the legacy default stream (it cannot be captured); host
+ * buffers must be page-locked.  The graph holds the plan's buffers and the
+ * transfers' addresses: launch it while they live, destroy it before the
+ * plan.  ibx_graph_launch replays the step on any stream; ibx_graph_kernels
+ * is the number of library kernels one launch runs. */
+typedef struct ibx_graph ibx_graph;
+int ibx_plan_graph(ibx_plan* plan, const ibx_transfer* in_X, int n_in_X, const ibx_transfer* in_Q, int n_in_Q,
+                   const ibx_transfer* out_Q, int n_out_Q, void* stream, ibx_graph** graph);
+int ibx_graph_launch(ibx_graph* graph, void* stream);
+int ibx_graph_kernels(const ibx_graph* graph);
+int ibx_graph_destroy(ibx_graph* graph);
 int ibx_plan_spread(ibx_plan* plan, void* stream);
 int ibx_plan_interpolate(ibx_plan* plan, void* stream);
 /* Status of the marker data seen by the last ibx_plan_bin (synchronises
@@ -454,7 +471,10 @@ int ibx_plan_get_interp_kernel(const ibx_plan* plan);
 /* How ibx_plan_step orders spread and interpolation after the binning (no
  * reference counterpart; chosen by the autotuner): 1 = concurrently, the
  * interpolation on a stream of the plan forked from and joined back to the
- * caller's stream (default); 0 = one after the other on the caller's
+ * caller's stream, the spread's stream of the device's greatest priority
+ * (default); 3 = concurrently with both streams of the same priority (which
+ * suits some marker sets better: the interpolation's loads then share the
+ * SMs evenly with the spread); 0 = one after the other on the caller's
  * stream, the interpolation first; 2 = both in one persistent launch on the caller's stream, whose
  * blocks take the dense spread's work items, the interpolation of the same
  * items, the interpolation of the other markers and then the per-visit

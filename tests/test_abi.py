@@ -70,6 +70,18 @@ def test_plan_knobs_reject_a_null_plan(libibx):
     assert L.ibx_plan_set_tuning(None, 128, 32, 2) == E_ARG
     L.ibx_plan_step_io.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p, ctypes.c_int] * 3 + [ctypes.c_void_p]
     assert L.ibx_plan_step_io(None, None, 0, None, 0, None, 0, None) == E_ARG
+    # the graph entry points: no plan, no graph pointer or the legacy stream
+    L.ibx_plan_graph.argtypes = ([ctypes.c_void_p] + [ctypes.c_void_p, ctypes.c_int] * 3 +
+                                 [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)])
+    h = ctypes.c_void_p(1234)
+    assert L.ibx_plan_graph(None, None, 0, None, 0, None, 0, ctypes.c_void_p(1), ctypes.byref(h)) == E_ARG
+    assert h.value is None  # cleared before the arguments are refused
+    assert L.ibx_plan_graph(None, None, 0, None, 0, None, 0, ctypes.c_void_p(1), None) == E_ARG
+    for name in ("ibx_graph_launch", "ibx_graph_kernels", "ibx_graph_destroy"):
+        getattr(L, name).argtypes = [ctypes.c_void_p] + ([ctypes.c_void_p] if name == "ibx_graph_launch" else [])
+    assert L.ibx_graph_launch(None, None) == E_ARG
+    assert L.ibx_graph_kernels(None) == -1
+    assert L.ibx_graph_destroy(None) == 0
 
 
 def test_force_entry_points_validate_on_the_host(libibx):

@@ -361,12 +361,13 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1, 2])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
 @pytest.mark.parametrize("interp_form", [0, 1, 2, 3, 4])
 def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_form, step_mode):
-    """ibx_plan_step (spread and interpolation on two streams, or one after
-    the other; the marker-order interpolation forked before the counting
-    sort) gives the oracle's answer, step after step."""
+    """ibx_plan_step (spread and interpolation on two streams, the spread's
+    first or both of one priority, or one after the other, or fused; the
+    marker-order interpolation forked before the counting sort) gives the
+    oracle's answer, step after step."""
     rng = np.random.default_rng(61 + dim)
     N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
     n = 2500
@@ -454,7 +455,7 @@ def test_fused_step_matches_oracle_and_separate_launches(ibx, oracle, kernel, di
 
 @pytest.mark.parametrize("x_source", ["pinned", "device"])
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1, 2])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
 @pytest.mark.parametrize("interp_form", [1, 2])
 def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, interp_form, x_source):
     """ibx_plan_step_io moves positions and forces in from pinned host memory
@@ -515,6 +516,63 @@ def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, in
         assert plan.status() == ibx.OK
         check(X2, F2)
     del g
+    plan.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("with_io", [False, True])
+def test_plan_graph_replays_the_step(ibx, oracle, dim, step_mode, with_io):
+    """ibx_plan_graph: a step (or a step with its host transfers) captured
+    into a graph instantiated with the plan's stream priorities, launched on
+    the current stream with new forces and positions: the oracle's answer at
+    every launch, the graph's kernel count that of an eager step."""
+    rng = np.random.default_rng(191 + dim + 3 * step_mode + 10 * with_io)
+    N = [24, 20, 16][:dim] if dim == 3 else [40, 36]
+    n = 2500
+    u = rng.standard_normal([dim] + list(N)[::-1])
+    X_t = torch.zeros(n * dim, dtype=torch.float64, device="cuda")
+    f_t = [torch.zeros(list(N)[::-1], dtype=torch.float32, device="cuda") for _ in range(dim)]
+    u_t = [torch.tensor(u[a], dtype=torch.float32, device="cuda") for a in range(dim)]
+    F_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    U_t = torch.zeros(n * dim, dtype=torch.float32, device="cuda")
+    Xh = torch.zeros(n * dim, dtype=torch.float64).pin_memory()
+    Fh = torch.zeros(n * dim, dtype=torch.float32).pin_memory()
+    Uh = torch.zeros(n * dim, dtype=torch.float32).pin_memory()
+    mk = lambda q, Q: ibx.make_problem(dim, ibx.SIDE, ibx.MODE_PERIODIC, [0] * dim, [v - 1 for v in N],
+                                       [1.0 / v for v in N], [0.0] * dim, [1.0] * dim, q, X_t, Q)
+    plan = ibx.Plan(mk(f_t, F_t), "IB_4", ibx.MIXED, interp_problems=[mk(u_t, U_t)])
+    plan.interp_kernel = 1
+    plan.step_mode = step_mode
+    io = dict(in_X=[(X_t, Xh)], in_Q=[(F_t, Fh)], out_Q=[(Uh, U_t)]) if with_io else {}
+    X_t.copy_(torch.tensor(seam_markers(rng, n, dim)))
+    l0 = ibx.kernel_launches()
+    plan.step()
+    eager_kernels = ibx.kernel_launches() - l0
+    torch.cuda.synchronize()
+    g = plan.graph(**io)
+    assert g.kernels == eager_kernels
+    for rep in range(2):
+        X2 = seam_markers(rng, n, dim)
+        F2 = rng.standard_normal(n * dim)
+        if with_io:
+            Xh.copy_(torch.tensor(X2))
+            Fh.copy_(torch.tensor(F2, dtype=torch.float32))
+        else:
+            X_t.copy_(torch.tensor(X2))
+            F_t.copy_(torch.tensor(F2, dtype=torch.float32))
+        for t in f_t:
+            t.zero_()
+        torch.cuda.synchronize()
+        g.launch()
+        torch.cuda.synchronize()
+        assert plan.status() == ibx.OK
+        f_ref, U_ref = oracle.periodic_problem(dim, N, "IB_4", X2, F=F2, u=u, centering=1)
+        f = np.stack([t.double().cpu().numpy() for t in f_t])
+        U = Uh if with_io else U_t
+        assert cases.rel_err(f, f_ref) <= MIXED_TOL
+        assert cases.rel_err(U.double().cpu().numpy(), U_ref) <= MIXED_TOL
+    g.close()
     plan.close()
 
 
