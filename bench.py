@@ -349,13 +349,13 @@ def tile_index(X, N, edges):
 
 def pick_io_mode(plan, step_e2e, timed, steps, recapture=None):
     """Step mode of the end-to-end step (bin + spread + interpolate with
-    their host transfers): the plan's own mode, the concurrent modes (the
-    interpolation's stream first, as its values go out, or both streams of
-    one priority), or mode 0 (interpolation first, its values' copy beside
-    the spread), whichever measures fastest; leaves the plan (and the
-    captured graph) in that mode."""
+    their host transfers): the plan's own mode, the concurrent modes (with
+    values going out the interpolation's stream comes first in modes 1 and
+    4; both of one priority in mode 3), or mode 0 (interpolation first, its
+    values' copy beside the spread), whichever measures fastest; leaves the
+    plan (and the captured graph) in that mode."""
     best = None
-    for m in dict.fromkeys([plan.step_mode, 1, 3, 0]):
+    for m in dict.fromkeys([plan.step_mode, 1, 3, 4, 0]):
         plan.step_mode = m
         if recapture:
             recapture()

@@ -454,7 +454,7 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     // Interpolation in marker order needs only the stencil records: in the
     // concurrent mode it forks as soon as they exist, beside the counting
     // sort; the other forms fork after the whole binning.
-    const bool concurrent = plan->step_mode == 1 || plan->step_mode == 3;
+    const bool concurrent = plan->step_mode == 1 || plan->step_mode == 3 || plan->step_mode == 4;
     const bool early = concurrent && plan->D.interp_form == 2;
     // the visit placement is left out of the binning in the concurrent
     // modes: it runs beside the dense-tile spread and the interpolation,
@@ -510,10 +510,12 @@ plan_step(ibx_plan* plan, cudaStream_t s, const ibx_transfer* in_X, int n_in_X, 
     // spread, runs on the stream of greatest priority -- unless the
     // interpolated values are copied out, then the interpolation does, so
     // that the copy runs beside the rest of the spread instead of after it.
-    // Mode 3: both on streams of the least priority.
+    // Mode 3: both on streams of the least priority.  Mode 4: the
+    // interpolation's stream first.
     const bool level = plan->step_mode == 3;
-    cudaStream_t s_int = level ? plan->side : out ? plan->spread_s : plan->side;
-    cudaStream_t s_spr = level ? plan->level : out ? plan->side : plan->spread_s;
+    const bool interp_first = out || plan->step_mode == 4;
+    cudaStream_t s_int = level ? plan->side : interp_first ? plan->spread_s : plan->side;
+    cudaStream_t s_spr = level ? plan->level : interp_first ? plan->side : plan->spread_s;
     if ((!early && cudaEventRecord(plan->ev_fork, s) != cudaSuccess) ||
         cudaStreamWaitEvent(s_int, plan->ev_fork, 0) != cudaSuccess)
         return wait_up(s) ? IBX_E_CUDA : IBX_E_CUDA;
@@ -723,7 +725,7 @@ ibx_plan_get_unit_cap(const ibx_plan* plan)
 int
 ibx_plan_set_step_mode(ibx_plan* plan, int mode)
 {
-    if (!plan || mode < 0 || mode > 3) return IBX_E_ARG;
+    if (!plan || mode < 0 || mode > 4) return IBX_E_ARG;
     plan->step_mode = mode;
     return IBX_OK;
 }

@@ -17,8 +17,8 @@ A plan has these knobs (``ibx_plan_set_tuning``, ``ibx_plan_set_visit_kernel``,
   markers evaluated from their home tile's region staged in shared memory
   (all of them, or the dense-homed ones);
 * ``step_mode``: spread and interpolation concurrent (the spread's stream
-  first, or both of one priority), one after the other, or fused into one
-  persistent launch in ``step``.
+  first, both of one priority, or the interpolation's first), one after the
+  other, or fused into one persistent launch in ``step``.
 
 The best setting depends on the marker distribution (clustered fibres favour
 regions, scattered markers favour visits), so it is measured: every
@@ -44,7 +44,7 @@ DEFAULT_CANDIDATES = {
     "dense_blocks_per_sm": (1, 2, 4),
     "visit_kernel": (0, 1, 2, 3),
     "interp_kernel": (0, 1, 2, 3, 4),
-    "step_mode": (1, 3, 0, 2),
+    "step_mode": (1, 3, 4, 0, 2),
     "unit_cap": (32, 16, 8),
 }
 

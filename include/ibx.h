@@ -472,9 +472,10 @@ int ibx_plan_get_interp_kernel(const ibx_plan* plan);
  * reference counterpart; chosen by the autotuner): 1 = concurrently, the
  * interpolation on a stream of the plan forked from and joined back to the
  * caller's stream, the spread's stream of the device's greatest priority
- * (default); 3 = concurrently with both streams of the same priority (which
- * suits some marker sets better: the interpolation's loads then share the
- * SMs evenly with the spread); 0 = one after the other on the caller's
+ * (default); 3 = concurrently with both streams of the same priority; 4 =
+ * concurrently with the interpolation's stream of the greatest priority (the
+ * shorter phase first, then the spread alone; the fastest order for some
+ * marker sets); 0 = one after the other on the caller's
  * stream, the interpolation first; 2 = both in one persistent launch on the caller's stream, whose
  * blocks take the dense spread's work items, the interpolation of the same
  * items, the interpolation of the other markers and then the per-visit

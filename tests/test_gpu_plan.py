@@ -361,11 +361,12 @@ def test_autotune_shape_keeps_the_fastest_plan(ibx, oracle):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("interp_form", [0, 1, 2, 3, 4])
 def test_plan_step_overlapped_equals_separate_calls(ibx, oracle, dim, interp_form, step_mode):
     """ibx_plan_step (spread and interpolation on two streams, the spread's
-    first or both of one priority, or one after the other, or fused; the
+    first, both of one priority or the interpolation's first, or one after
+    the other, or fused; the
     marker-order interpolation forked before the counting sort) gives the
     oracle's answer, step after step."""
     rng = np.random.default_rng(61 + dim)
@@ -455,7 +456,7 @@ def test_fused_step_matches_oracle_and_separate_launches(ibx, oracle, kernel, di
 
 @pytest.mark.parametrize("x_source", ["pinned", "device"])
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("interp_form", [1, 2])
 def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, interp_form, x_source):
     """ibx_plan_step_io moves positions and forces in from pinned host memory
@@ -520,7 +521,7 @@ def test_step_io_host_buffers_eager_and_captured(ibx, oracle, dim, step_mode, in
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-@pytest.mark.parametrize("step_mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("step_mode", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("with_io", [False, True])
 def test_plan_graph_replays_the_step(ibx, oracle, dim, step_mode, with_io):
     """ibx_plan_graph: a step (or a step with its host transfers) captured
