@@ -75,8 +75,8 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
     ``dense_blocks_per_sm``, ``unit_cap``); for plans with their own
     interpolation targets, the interpolation form jointly with the step mode
     (concurrent, serial or fused spread and interpolation), and then, under
-    each of the two fastest of those pairs, the split with the visit form and
-    the dense-kernel knobs once more.  Returns {"best": (item_units, dense_min,
+    each of the three fastest of those pairs, the split with the visit form
+    and the dense-kernel knobs once more.  Returns {"best": (item_units, dense_min,
     dense_blocks_per_sm), "visit_kernel": form, "interp_kernel": form or
     None, "step_mode": mode or None, "unit_cap": cap, "ms": t, "table":
     [((item_units, dense_min, dense_blocks_per_sm, visit_kernel,
@@ -142,12 +142,12 @@ def autotune(plan, reps=3, candidates=None, key=None, include_bin=True):
         stage3 = len(table)
         for ik, sm in itertools.product(cand["interp_kernel"], cand["step_mode"]):
             measure((iu, dm, bps, vk, ik, sm, cap))
-        # the spread knobs again under the two fastest interpolation forms and
-        # step modes: beside a concurrent interpolation fewer dense CTAs and
-        # another split between the spread kernels can be best, one after the
-        # other more
+        # the spread knobs again under the three fastest interpolation forms
+        # and step modes: beside a concurrent interpolation fewer dense CTAs
+        # and another split between the spread kernels can be best, one after
+        # the other more
         ranked = sorted(table[stage3:], key=lambda r: r[1])
-        pairs = list(dict.fromkeys((c[4], c[5]) for c, _ in ranked))[:2]
+        pairs = list(dict.fromkeys((c[4], c[5]) for c, _ in ranked))[:3]
         for ik, sm in pairs:
             for dm2, vk2 in itertools.product(cand["dense_min"], cand["visit_kernel"]):
                 measure((iu, dm2, bps, vk2, ik, sm, cap))
