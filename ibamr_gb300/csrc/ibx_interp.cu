@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(INTERP_THREADS) interp_chunks(const DevPlan D,
 template <int DIM, int K>
 __global__ void __launch_bounds__(INTERP_THREADS, 3) interp_chunks_sparse(const DevPlan D)
 {
-    chunk_body<DIM, K, false>(D, blockIdx.x * (long long)blockDim.x + threadIdx.x, SEL_SPARSE, 0);
+    chunk_body<DIM, K, false, true>(D, blockIdx.x * (long long)blockDim.x + threadIdx.x, SEL_SPARSE, 0);
 }
 
 // CTAs per SM the per-unit interpolation's registers are cut for: 3 in 3D

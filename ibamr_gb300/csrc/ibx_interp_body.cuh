@@ -53,6 +53,46 @@ separable_sum(const float (&w)[3][W], At at)
     return V;
 }
 
+// separable_sum over rows read as aligned 8-byte pairs: q0 points at the
+// even value at or before the stencil's first x (odd: the first x is the
+// pair's second value); the rows' cells along y and z are co[1], co[2].  The
+// same FP32 operations in the same order as separable_sum.
+template <int DIM, int W>
+__device__ __forceinline__ float
+separable_sum_pairs(const float (&w)[3][W], const float* q0, int odd, const int (&co)[3][W], long long n0,
+                    long long n01)
+{
+    constexpr int NP = W / 2 + 1; // pairs covering W values from an odd start
+    float V = 0.f;
+#pragma unroll
+    for (int i2 = 0; i2 < (DIM == 3 ? W : 1); ++i2)
+    {
+        float vy = 0.f;
+#pragma unroll
+        for (int i1 = 0; i1 < W; ++i1)
+        {
+            const float2* row = reinterpret_cast<const float2*>(q0 + (DIM == 3 ? co[2][i2] * n01 : 0) + co[1][i1] * n0);
+            float f[2 * NP];
+#pragma unroll
+            for (int j = 0; j < NP; ++j)
+            {
+                // the last pair only when it holds a stencil value (an odd
+                // start, or an odd width)
+                float2 v = make_float2(0.f, 0.f);
+                if (j < NP - 1 || odd || (W & 1)) v = __ldg(row + j);
+                f[2 * j] = v.x;
+                f[2 * j + 1] = v.y;
+            }
+            float vx = 0.f;
+#pragma unroll
+            for (int i0 = 0; i0 < W; ++i0) vx = fmaf(w[0][i0], odd ? f[i0 + 1] : f[i0], vx);
+            vy = fmaf(w[1][i1], vx, vy);
+        }
+        V = fmaf(DIM == 3 ? w[2][i2] : 1.f, vy, V);
+    }
+    return V;
+}
+
 // Kernel weights of component c of a record (w[d][0] = 1 beyond DIM).
 template <int DIM, int K>
 __device__ __forceinline__ void
@@ -95,8 +135,9 @@ stencil_cells(const PlanProb& P, const Rec& R, int c, int (&co)[3][W])
 // CACHE_OK: the W^d stencil values may be cached in registers across markers
 // sharing a stencil (interp_chunks); off where registers are scarce (the
 // fused step kernel takes only sparse-homed markers this way, which rarely
-// share stencils).
-template <int DIM, int K, bool CACHE_OK>
+// share stencils).  PAIRS: uncached six-value rows that do not wrap are read
+// as aligned 8-byte pairs (separable_sum_pairs).
+template <int DIM, int K, bool CACHE_OK, bool PAIRS = false>
 __device__ __forceinline__ void
 chunk_body(const DevPlan& D, long long tid, int select, int marker_order)
 {
@@ -164,9 +205,20 @@ chunk_body(const DevPlan& D, long long tid, int select, int marker_order)
         {
             int co[3][W];
             stencil_cells<DIM, W>(P, R, c, co);
-            V = separable_sum<DIM, W>(w, [&](int i0, int i1, int i2) {
-                return __ldg(q + (DIM == 3 ? co[2][i2] * n01 : 0) + co[1][i1] * n0 + co[0][i0]);
-            });
+            const int bx = (P.side && c == 0) ? R.bs(0) : R.bc(0);
+            // six-value rows that do not wrap, in a grid whose rows start
+            // 8-byte aligned: read as aligned pairs (three or four loads per
+            // row instead of six), the values picked by the row's parity; the
+            // same sums.  (For four-value rows the pairs measured slower in
+            // the concurrent step: they take more of the L1 the gather spread
+            // shares.)
+            if (PAIRS && W == 6 && bx + W <= P.N[0] && (P.N[0] & 1) == 0 &&
+                (reinterpret_cast<unsigned long long>(q) & 7ull) == 0)
+                V = separable_sum_pairs<DIM, W>(w, q + (bx & ~1), bx & 1, co, n0, n01);
+            else
+                V = separable_sum<DIM, W>(w, [&](int i0, int i1, int i2) {
+                    return __ldg(q + (DIM == 3 ? co[2][i2] * n01 : 0) + co[1][i1] * n0 + co[0][i0]);
+                });
         }
         static_cast<float*>(P.Qi)[(long long)P.Q_depth * (g - P.marker0) + c] = V;
     }
